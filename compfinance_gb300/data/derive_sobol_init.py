@@ -7,7 +7,9 @@ The library regenerates the full table from this compact data with the Joe-Kuo
 recurrence (compfinance_gb300/csrc/sobol_dirs.cpp), so the points are bit-identical
 without carrying the expanded table.  Usage:
 
-    python3 compfinance_gb300/data/derive_sobol_init.py [sobol.cpp] > compfinance_gb300/data/sobol_init.txt
+    python3 compfinance_gb300/data/derive_sobol_init.py [sobol.cpp] > compfinance_gb300/data/sobol_joe_kuo.inc
+
+The output is a C/C++ initializer list included by the library and by the oracle.
 """
 import re
 import sys
@@ -47,15 +49,17 @@ def main():
     path = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/sobol.cpp"
     dirs = parse(path)
     ndim = len(dirs[0])
-    print("# Joe-Kuo Sobol initialisation data, 'old' set, %d dimensions." % ndim)
-    print("# One line per dimension: s a m_1 ... m_s.  Dimension 0 is van der Corput (s=0).")
+    print("/* Joe-Kuo Sobol initialisation data ('old' set), %d dimensions." % ndim)
+    print(" * One entry per dimension: {s, a, {m_1, ..., m_s}}; dimension 0 is van der Corput (s=0).")
+    print(" * Generated by compfinance_gb300/data/derive_sobol_init.py. */")
+    print("#define CF_SOBOL_MAX_DIM %d" % ndim)
     for d in range(ndim):
         col = [dirs[i][d] for i in range(32)]
         if all(col[k] == 1 << (31 - k) for k in range(32)):
-            print("0 0")
+            print("{0, 0, {0}},")
             continue
         s, a, m = derive(col)
-        print(s, a, *m)
+        print("{%d, %d, {%s}}," % (s, a, ", ".join(str(x) for x in m)))
 
 
 if __name__ == "__main__":

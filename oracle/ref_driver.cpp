@@ -176,8 +176,9 @@ int main()
         else if (cmd == "sobol_dirhash")  // per-dimension FNV-1a hash of the 32 direction numbers
         {
             const unsigned* const* dir = getjkDir();
-            std::vector<double> h(1111);
-            for (size_t d = 0; d < 1111; ++d)
+            // The tables hold 1101 dimensions (sobol.cpp), although sobol.h:93 says 1111.
+            std::vector<double> h(1101);
+            for (size_t d = 0; d < 1101; ++d)
             {
                 unsigned long long x = 1469598103934665603ULL;
                 for (int i = 0; i < 32; ++i)

@@ -220,6 +220,7 @@ def mc_cases(models, products):
         ("bs_uoc_mrg", "bs", "uoc", "risk", 0, 1024, 0),
         ("bs_uoc_mrg_p1", "bs", "uoc", "risk", 0, 1024, 1),
         ("bs_europeans_multi", "bs_spotmeasure", "europeans", "multi", 1, 1024, None),
+    ] + [(f"bs_europeans_each_{k}", "bs_spotmeasure", "europeans", "risk", 1, 1024, k) for k in range(12)] + [
         ("dup20x10_uoc", "dup20x10", "uoc", "risk", 0, 2048, 0),
         ("c2_dup60x30_uoc", "dup60x30", "uoc", "risk", 0, 4096, 0),
         ("c2_dup60x30_uoc_p1", "dup60x30", "uoc", "risk", 0, 2048, 1),

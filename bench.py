@@ -1,0 +1,280 @@
+#!/usr/bin/env python3
+"""Benchmark of the Dupire up-and-out AAD-risk workload on one GB300.
+
+Workload (one "step"): AADriskOne of the smoothed up-and-out call (K=120, B=150, 1%
+smoothing, T=3y, 156 weekly monitoring dates) on a Dupire local-vol surface of 60 spots x 30
+times, mrg32k3a(12345, 1234), 2^22 paths, FP32 path arithmetic with exact fixed-point
+accumulation: price plus the 1801 risks (spot + every local-vol node).  The same run in the
+FP64 form is timed beside it (the FP32-vs-FP64 ratio and their difference in MC standard
+errors are reported).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line.  `value` is device-timed throughput with the model resident in HBM;
+`e2e` goes through the C ABI with host buffers each step (putDupire upload + risk + result
+download).  `--impl reference` times the CPU restatement of the reference's algorithm
+(oracle/, hand-written per-path adjoint, all host threads) on a bounded sample of the same
+workload.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from compfinance_gb300 import workloads as W  # noqa: E402
+
+METRIC = "AAD-risk paths/s (Dupire barrier), FP32 vs FP64 at equal error; serve p99 ms"
+NPATH = 1 << 22
+GRID = (60, 30)
+FLOPS_PER_PATH_STEP = 53.0   # algorithmic FP work of value + adjoint per path-step (mrg32k3a)
+CONFIG = {
+    "workload": "dupire_uoc_aad_risk_60x30_156steps_2^22paths_fp32path",
+    "model": "Dupire local vol 60x30 (50-200 log-spaced x 0.1-3.0y), seeded synthetic surface",
+    "product": "up-and-out call K=120 B=150 smooth 1% T=3y weekly (156 steps)",
+    "rng": "mrg32k3a(12345,1234) antithetic",
+    "paths": NPATH,
+    "risks": 1801,
+    "l2": "flushed between steps (256 MiB write outside the per-step events); per-thread reverse-sweep "
+          "scratch of ~0.4 GB also exceeds L2",
+}
+
+
+def env_rank():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return json.load(fh)
+    except OSError:
+        return {}
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    def __init__(self, path):
+        self.path = path
+        self.proc = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-lms", "100"], stdout=self.fh, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait()
+            self.fh.close()
+
+    def summary(self):
+        try:
+            rows = [r.split(", ") for r in open(self.path).read().strip().splitlines()]
+        except OSError:
+            return None
+        rows = [r for r in rows if len(r) >= 9]
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = max(float(r[2]) for r in rows if r[2].replace(".", "").isdigit())
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].strip().lower() == "active"})
+        loaded = [s for s in sm if s > 0.5 * mx] or sm
+        return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": mx, "reasons": reasons, "samples": len(rows)}
+
+
+def cpu_baseline(seconds=12.0, threads=None):
+    """The oracle's hand-written adjoint (multi-threaded) on a bounded sample of the workload."""
+    import oracle as O
+    s, t, v = W.dupire_surface(*GRID)
+    u = W.UOC_BARRIER
+    m = O.Model(dict(kind="dupire", spot=W.DUPIRE_SPOT, spots=s, times=t, vols=v, maxdt=W.DUPIRE_MAXDT))
+    p = O.Product(dict(kind="uoc", strike=u["strike"], barrier=u["barrier"], maturity=u["maturity"],
+                       freq=u["monitor_freq"], smooth=u["smooth"], callput=0))
+    threads = threads or os.cpu_count() or 1
+    w = np.array([1.0, 0.0])
+    n = 1 << 12
+    t0 = time.perf_counter()
+    O.risk(m, p, 0, n, w, fast=True, threads=threads)
+    dt = time.perf_counter() - t0
+    n = int(min(1 << 23, max(n, n * seconds / max(dt, 1e-3))))
+    n -= n % 2
+    t0 = time.perf_counter()
+    O.risk(m, p, 0, n, w, fast=True, threads=threads)
+    dt = time.perf_counter() - t0
+    return {"value": n / dt, "unit": "paths/s", "cores": threads, "kind": "port",
+            "sample": f"{n} paths of the same workload (FP64, hand-written adjoint), {dt:.2f} s"}
+
+
+def run_reference(args):
+    rank, world, _ = env_rank()
+    if rank != 0:
+        return 0
+    cb = cpu_baseline()
+    out = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "paths/s", "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "dtype": "f64",
+           "data": "synthetic", "config": CONFIG, "cpu_baseline": cb,
+           "e2e": {"value": cb["value"], "unit": "paths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    from compfinance_gb300 import Engine, NumericalParam
+
+    rank, world, local = env_rank()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    stream = torch.cuda.Stream()       # a real stream handle (the legacy default stream is 0)
+    torch.cuda.set_stream(stream)
+    eng = Engine(local)
+    eng.set_stream(stream.cuda_stream)
+    s, t, v = W.dupire_surface(*GRID)
+    u = W.UOC_BARRIER
+    eng.putDupire(W.DUPIRE_SPOT, s, t, v, W.DUPIRE_MAXDT, "dupire")
+    eng.putBarrier(u["strike"], u["barrier"], u["maturity"], u["monitor_freq"], u["smooth"], 0, "uoc")
+    npay, npar, dim = eng.shapes("dupire", "uoc")
+    # Each rank simulates its own 2^22 paths (independent seeds): weak scaling, no exchange.
+    seed1 = W.MRG_SEEDS[0] + 7919 * rank
+    num32 = NumericalParam(numPath=NPATH, precision="fp32", seed1=seed1)
+    num64 = NumericalParam(numPath=NPATH, precision="fp64", seed1=seed1)
+    flush = torch.empty(64 << 20, dtype=torch.float32, device="cuda")
+
+    def timed(num, steps, warmup):
+        for _ in range(warmup):
+            eng.enqueue("dupire", "uoc", num, risk=True)
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        launches = 0
+        w0 = time.perf_counter()
+        for k in range(steps):
+            flush.fill_(float(k))
+            evs[k][0].record(stream)
+            launches += eng.enqueue("dupire", "uoc", num, risk=True)
+            evs[k][1].record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - w0
+        ms = [a.elapsed_time(b) for a, b in evs]
+        tot = sum(ms) / 1e3
+        if world > 1:
+            tt = torch.tensor([tot], device="cuda")
+            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+            tot = float(tt.item())
+        return tot, ms, launches, wall
+
+    os.makedirs(os.path.join(ROOT, "gpurun_out"), exist_ok=True)
+    with Clocks(os.path.join(ROOT, "gpurun_out", f"bench_clocks_r{rank}.csv")) as ck:
+        t32, ms32, launches, wall32 = timed(num32, args.steps, args.warmup)
+    clocks = ck.summary()
+    v32, e32, agg32, r32 = eng.fetch(npay, npar)
+    steps64 = max(2, min(args.steps, 4))
+    t64, ms64, _, _ = timed(num64, steps64, 1)
+    v64, e64, agg64, r64 = eng.fetch(npay, npar)
+
+    # equal-error check: FP32 vs FP64 on the same paths, in Monte Carlo standard errors
+    se = []
+    for k in range(8):
+        eng.enqueue("dupire", "uoc", NumericalParam(numPath=NPATH // 4, precision="fp32", seed1=1000 + k, seed2=77 + k),
+                    risk=True)
+        se.append(eng.fetch(npay, npar)[3])
+    se = np.std(np.array(se), axis=0, ddof=1) / 2.0  # std at N/4 -> standard error at N
+    mask = se > 1e-3 * np.abs(r64).max()
+    risk_err_se = float(np.max(np.abs(r32 - r64)[mask] / se[mask]))
+    price_err_se = float(abs(v32[0] - v64[0]) / e64[0])
+
+    # end to end through the C ABI with host buffers
+    h0, d0 = eng.transfer_stats()
+    torch.cuda.synchronize()
+    ke = max(2, min(args.steps, 5))
+    w0 = time.perf_counter()
+    for k in range(ke):
+        eng.putDupire(W.DUPIRE_SPOT, s, t, v, W.DUPIRE_MAXDT, "dupire")
+        eng.AADriskOne("dupire", "uoc", num32)
+    e2e_t = (time.perf_counter() - w0) / ke
+    h1, d1 = eng.transfer_stats()
+
+    steps_tot = NPATH * dim
+    per_step = t32 / args.steps
+    value = world * NPATH / per_step
+    pk = peaks()
+    sm_max = float(pk.get("sm_max_mhz", 2070.0))
+    peak_fp32 = 152 * 128 * 2 * sm_max * 1e6 / 1e12
+    achieved = FLOPS_PER_PATH_STEP * steps_tot / per_step / 1e12
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        try:
+            tr = json.load(open(tpath))
+            traffic = tr.get("bytes_per_path_step_fp32_risk", None)
+            traffic = traffic * steps_tot if traffic else None
+        except (OSError, ValueError):
+            traffic = None
+    out = {
+        "metric": METRIC, "value": value, "unit": "paths/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": per_step * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": CONFIG,
+        "path_steps_per_s": value * dim,
+        "fp64": {"value": world * NPATH / (t64 / steps64), "unit": "paths/s", "ms_per_step": t64 / steps64 * 1e3,
+                 "steps": steps64},
+        "fp32_over_fp64": (t64 / steps64) / per_step,
+        "equal_error": {"price_fp32_minus_fp64_in_stderr": price_err_se,
+                        "max_risk_fp32_minus_fp64_in_stderr": risk_err_se,
+                        "price": float(v64[0]), "price_stderr": float(e64[0])},
+        "roofline": {"bound": "fp32_simt", "achieved": achieved, "peak": peak_fp32, "unit": "TFLOP/s",
+                     "frac": achieved / peak_fp32, "traffic": traffic,
+                     "peak_source": "152 SM x 128 FP32 lanes x 2 x sm_max_mhz of MEASURED_PEAKS.json "
+                                    "(no tensor-core or HBM bound applies)",
+                     "flops_per_path_step": FLOPS_PER_PATH_STEP},
+        "e2e": {"value": world * NPATH / e2e_t, "unit": "paths/s", "h2d_bytes_per_step": (h1 - h0) // ke,
+                "d2h_bytes_per_step": (d1 - d0) // ke},
+        "gpu_launches": launches,
+        "clocks": clocks,
+        "step_ms": [round(x, 4) for x in ms32],
+    }
+    if rank == 0 and not args.no_cpu:
+        out["cpu_baseline"] = cpu_baseline()
+    if rank == 0:
+        print(json.dumps(out))
+    eng.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,283 @@
+"""ctypes binding of libcfgpu.so under the reference's entry-point names (main.h, store.h)."""
+import ctypes
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(HERE, "libcfgpu.so")
+_dp = ctypes.POINTER(ctypes.c_double)
+_lib = None
+
+
+def library_path():
+    return _LIB_PATH
+
+
+class CfError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"cfgpu error {code}: {msg}")
+        self.code = code
+
+
+class CfNumParam(ctypes.Structure):
+    _fields_ = [("parallel", ctypes.c_int), ("useSobol", ctypes.c_int), ("numPath", ctypes.c_int),
+                ("seed1", ctypes.c_int), ("seed2", ctypes.c_int), ("precision", ctypes.c_int)]
+
+
+class CfIvs(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int), ("spot", ctypes.c_double), ("p", ctypes.c_double * 4)]
+
+
+def lib():
+    """Load libcfgpu.so; raises if it has not been built (there is no fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIB_PATH):
+            raise CfError(-7, f"{_LIB_PATH} missing: build it with __graft_entry__.build()")
+        _lib = ctypes.CDLL(_LIB_PATH)
+        _lib.cf_create.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]
+    return _lib
+
+
+def _check(rc):
+    if rc != 0:
+        buf = ctypes.create_string_buffer(4096)
+        lib().cf_last_error(buf, ctypes.c_size_t(4096))
+        raise CfError(rc, buf.value.decode(errors="replace"))
+
+
+def _arr(x, dtype=np.float64):
+    a = np.ascontiguousarray(np.asarray(x, dtype=dtype))
+    return a
+
+
+def _p(a):
+    return a.ctypes.data_as(_dp)
+
+
+@dataclass
+class NumericalParam:
+    """main.h:33-40, plus the precision of the path arithmetic ('fp64' or 'fp32')."""
+    parallel: bool = True
+    useSobol: bool = False
+    numPath: int = 1 << 16
+    seed1: int = 12345
+    seed2: int = 1234
+    precision: str = "fp64"
+
+    def c(self):
+        return CfNumParam(int(self.parallel), int(self.useSobol), int(self.numPath), int(self.seed1),
+                          int(self.seed2), 1 if self.precision == "fp32" else 0)
+
+
+class Engine:
+    """One context on one GPU: the store plus the entry points of main.h."""
+
+    def __init__(self, device=0):
+        h = ctypes.c_void_p()
+        _check(lib().cf_create(int(device), ctypes.byref(h)))
+        self._h = h
+
+    def close(self):
+        if self._h:
+            lib().cf_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream_ptr):
+        _check(lib().cf_set_stream(self._h, ctypes.c_void_p(stream_ptr)))
+
+    def synchronize(self):
+        _check(lib().cf_synchronize(self._h))
+
+    def transfer_stats(self):
+        h, d = ctypes.c_uint64(), ctypes.c_uint64()
+        _check(lib().cf_transfer_stats(self._h, ctypes.byref(h), ctypes.byref(d)))
+        return h.value, d.value
+
+    # ---- store (store.h) ----------------------------------------------------------------
+    def putBlackScholes(self, spot, vol, qSpot, rate, div, id):
+        _check(lib().cf_put_black_scholes(self._h, ctypes.c_double(spot), ctypes.c_double(vol), int(bool(qSpot)),
+                                          ctypes.c_double(rate), ctypes.c_double(div), id.encode()))
+        return id
+
+    def putDupire(self, spot, spots, times, vols, maxDt, id):
+        s, t = _arr(spots), _arr(times)
+        v = _arr(vols).reshape(-1)
+        if v.size != s.size * t.size:
+            raise CfError(-1, "putDupire: vols must be len(spots) x len(times)")
+        _check(lib().cf_put_dupire(self._h, ctypes.c_double(spot), _p(s), len(s), _p(t), len(t), _p(v),
+                                   ctypes.c_double(maxDt), id.encode()))
+        return id
+
+    def putEuropean(self, strike, exerciseDate, settlementDate=None, id="european"):
+        if settlementDate is None:
+            settlementDate = exerciseDate
+        _check(lib().cf_put_european(self._h, ctypes.c_double(strike), ctypes.c_double(exerciseDate),
+                                     ctypes.c_double(settlementDate), id.encode()))
+        return id
+
+    def putBarrier(self, strike, barrier, maturity, monitorFreq, smooth, callPut, id):
+        _check(lib().cf_put_barrier(self._h, ctypes.c_double(strike), ctypes.c_double(barrier),
+                                    ctypes.c_double(maturity), ctypes.c_double(monitorFreq), ctypes.c_double(smooth),
+                                    int(bool(callPut)), id.encode()))
+        return id
+
+    def putEuropeans(self, maturities, strikes, id):
+        m, k = _arr(maturities), _arr(strikes)
+        _check(lib().cf_put_europeans(self._h, _p(m), _p(k), len(m), id.encode()))
+        return id
+
+    def _labels(self, fn, key):
+        n, need = ctypes.c_int(), ctypes.c_size_t()
+        _check(fn(self._h, key.encode(), None, ctypes.c_size_t(0), ctypes.byref(n), ctypes.byref(need)))
+        buf = ctypes.create_string_buffer(need.value)
+        _check(fn(self._h, key.encode(), buf, need, ctypes.byref(n), ctypes.byref(need)))
+        s = buf.value.decode()
+        return s.split("\n") if s else []
+
+    def payoffLabels(self, productId):
+        return self._labels(lib().cf_payoff_labels, productId)
+
+    def parameterLabels(self, modelId):
+        return self._labels(lib().cf_parameter_labels, modelId)
+
+    def shapes(self, modelId, productId):
+        a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        _check(lib().cf_shapes(self._h, modelId.encode(), productId.encode(), ctypes.byref(a), ctypes.byref(b),
+                               ctypes.byref(c)))
+        return a.value, b.value, c.value
+
+    # ---- entry points (main.h) -----------------------------------------------------------
+    def value(self, modelId, productId, num):
+        npay, _, _ = self.shapes(modelId, productId)
+        v, e = np.zeros(npay), np.zeros(npay)
+        nc = num.c()
+        _check(lib().cf_value(self._h, modelId.encode(), productId.encode(), ctypes.byref(nc), _p(v), _p(e)))
+        return dict(identifiers=self.payoffLabels(productId), values=v, stderrs=e)
+
+    def AADriskOne(self, modelId, productId, num, riskPayoff=""):
+        npay, npar, _ = self.shapes(modelId, productId)
+        v, r = np.zeros(npay), np.zeros(npar)
+        rv = ctypes.c_double()
+        nc = num.c()
+        _check(lib().cf_aad_risk_one(self._h, modelId.encode(), productId.encode(), ctypes.byref(nc),
+                                     riskPayoff.encode(), _p(v), ctypes.byref(rv), _p(r)))
+        return dict(payoffIds=self.payoffLabels(productId), payoffValues=v, riskPayoffValue=rv.value,
+                    paramIds=self.parameterLabels(modelId), risks=r)
+
+    def AADriskAggregate(self, modelId, productId, notionals, num):
+        npay, npar, _ = self.shapes(modelId, productId)
+        labels = self.payoffLabels(productId)
+        w = np.zeros(npay)
+        if isinstance(notionals, dict):
+            for lab, x in notionals.items():
+                if lab not in labels:
+                    raise CfError(-2, "AADriskAggregate() : payoff not found")
+                w[labels.index(lab)] = x
+        else:
+            w[:] = notionals
+        v, r = np.zeros(npay), np.zeros(npar)
+        agg = ctypes.c_double()
+        nc = num.c()
+        _check(lib().cf_aad_risk_aggregate(self._h, modelId.encode(), productId.encode(), _p(w), ctypes.byref(nc),
+                                           _p(v), ctypes.byref(agg), _p(r)))
+        return dict(payoffIds=labels, payoffValues=v, riskPayoffValue=agg.value,
+                    paramIds=self.parameterLabels(modelId), risks=r)
+
+    def AADriskMulti(self, modelId, productId, num):
+        npay, npar, _ = self.shapes(modelId, productId)
+        v, r = np.zeros(npay), np.zeros(npar * npay)
+        nc = num.c()
+        _check(lib().cf_aad_risk_multi(self._h, modelId.encode(), productId.encode(), ctypes.byref(nc), _p(v),
+                                       _p(r)))
+        return dict(payoffs=self.payoffLabels(productId), params=self.parameterLabels(modelId), values=v,
+                    risks=r.reshape(npar, npay))
+
+    @staticmethod
+    def ivs(kind, spot, params):
+        s = CfIvs()
+        s.kind = 0 if kind in ("param", 0) else 1
+        s.spot = spot
+        for i, x in enumerate(params):
+            s.p[i] = x
+        return s
+
+    def dupireCalib(self, ivs, inclSpots, maxDs, inclTimes, maxDtVol):
+        a, b = _arr(inclSpots), _arr(inclTimes)
+        nS, nT = ctypes.c_int(), ctypes.c_int()
+        _check(lib().cf_dupire_calib(self._h, ctypes.byref(ivs), _p(a), len(a), ctypes.c_double(maxDs), _p(b), len(b),
+                                     ctypes.c_double(maxDtVol), ctypes.byref(nS), ctypes.byref(nT), None, None, None))
+        s, t, lv = np.zeros(nS.value), np.zeros(nT.value), np.zeros(nS.value * nT.value)
+        _check(lib().cf_dupire_calib(self._h, ctypes.byref(ivs), _p(a), len(a), ctypes.c_double(maxDs), _p(b), len(b),
+                                     ctypes.c_double(maxDtVol), ctypes.byref(nS), ctypes.byref(nT), _p(s), _p(t),
+                                     _p(lv)))
+        return dict(spots=s, times=t, lVols=lv.reshape(nS.value, nT.value))
+
+    def dupireSuperbucket(self, ivs, spot, maxDt, productId, notionals, inclSpots, maxDs, inclTimes, maxDtVol,
+                          strikes, mats, num, refSeeding=False):
+        npay = len(self.payoffLabels(productId))
+        labels = self.payoffLabels(productId)
+        w = np.zeros(npay)
+        if isinstance(notionals, dict):
+            for lab, x in notionals.items():
+                w[labels.index(lab)] = x
+        else:
+            w[:] = notionals
+        a, b = _arr(inclSpots), _arr(inclTimes)
+        k, m = _arr(strikes), _arr(mats)
+        nS, nT = ctypes.c_int(), ctypes.c_int()
+        _check(lib().cf_dupire_calib(self._h, ctypes.byref(ivs), _p(a), len(a), ctypes.c_double(maxDs), _p(b), len(b),
+                                     ctypes.c_double(maxDtVol), ctypes.byref(nS), ctypes.byref(nT), None, None, None))
+        vega = np.zeros(len(k) * len(m))
+        micro = np.zeros(nS.value * nT.value)
+        val, dl = ctypes.c_double(), ctypes.c_double()
+        nc = num.c()
+        _check(lib().cf_dupire_superbucket(self._h, ctypes.byref(ivs), ctypes.c_double(spot), ctypes.c_double(maxDt),
+                                           productId.encode(), _p(w), _p(a), len(a), ctypes.c_double(maxDs), _p(b),
+                                           len(b), ctypes.c_double(maxDtVol), _p(k), len(k), _p(m), len(m),
+                                           ctypes.byref(nc), int(bool(refSeeding)), ctypes.byref(val),
+                                           ctypes.byref(dl), _p(vega), _p(micro)))
+        return dict(value=val.value, delta=dl.value, strikes=k, mats=m, vega=vega.reshape(len(k), len(m)),
+                    microbucket=micro.reshape(nS.value, nT.value))
+
+    # ---- RNG access --------------------------------------------------------------------------
+    def sobolPoints(self, dim, firstPath, nPaths):
+        out = np.zeros(nPaths * dim, dtype=np.uint32)
+        _check(lib().cf_sobol_points(self._h, int(dim), ctypes.c_int64(firstPath), int(nPaths),
+                                     out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))))
+        return out.reshape(nPaths, dim)
+
+    def mrgState(self, seed1, seed2, dim, firstPath):
+        out = np.zeros(6, dtype=np.uint32)
+        _check(lib().cf_mrg_state(self._h, ctypes.c_uint(seed1), ctypes.c_uint(seed2), int(dim),
+                                  ctypes.c_int64(firstPath), out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))))
+        return out
+
+    def gaussians(self, useSobol, seed1, seed2, dim, firstPath, nPaths):
+        out = np.zeros(nPaths * dim)
+        _check(lib().cf_gaussians(self._h, int(bool(useSobol)), ctypes.c_uint(seed1), ctypes.c_uint(seed2), int(dim),
+                                  ctypes.c_int64(firstPath), int(nPaths), _p(out)))
+        return out.reshape(nPaths, dim)
+
+    # ---- device-resident launches ------------------------------------------------------------
+    def enqueue(self, modelId, productId, num, risk=True, weights=None):
+        w = None if weights is None else _arr(weights)
+        n = ctypes.c_int()
+        nc = num.c()
+        _check(lib().cf_enqueue(self._h, modelId.encode(), productId.encode(), ctypes.byref(nc), int(bool(risk)),
+                                None if w is None else _p(w), ctypes.byref(n)))
+        return n.value
+
+    def fetch(self, npay, nparam=0):
+        v, e, r = np.zeros(npay), np.zeros(npay), np.zeros(max(nparam, 1))
+        agg = ctypes.c_double()
+        _check(lib().cf_fetch_result(self._h, _p(v), _p(e), ctypes.byref(agg), _p(r) if nparam else None))
+        return v, e, agg.value, r[:nparam]

@@ -1,0 +1,28 @@
+// Parameters of the calibration kernels (calib_kernels.cu), shared with calib.cpp.
+#pragma once
+
+namespace cf {
+
+struct CalibParams
+{
+    int ivsKind;      // 0 parametric, 1 Merton
+    double spot;
+    double ivp[4];
+    int nS, nT;
+    const double* spots;
+    const double* times;
+    const int* il;    // [nT] first / last spot index inside +-2.5 std
+    const int* ih;
+    int nK, nM;       // risk view
+    const double* rvK;
+    const double* rvM;
+    double* c;        // [nT][nS][5] calls
+    double* vega;     // [nT][nS][5] d call / d vol
+    double* lvT;      // [nT][nS] local vols, maturity-major
+    const double* seed;   // [nS][nT] adjoint of each local vol (extrapolation folded in)
+    long long* acc;       // [nK*nM][2] fixed-point accumulators of d / d spread
+};
+
+int launch_calib(const CalibParams& p, int adjoint, void* stream);
+
+}  // namespace cf

@@ -1,0 +1,116 @@
+// Launch descriptors shared by the host planner (engine.cpp) and the CUDA kernels.
+//
+// A (model, product) pair is lowered once into flat device tables: the simulation timeline,
+// per-step model coefficients, the event map from simulation steps to product dates, and
+// the product's constants.  Kernels never see strings, virtual calls or host pointers.
+#pragma once
+#include <cstdint>
+
+namespace cf {
+
+enum ModelKind : int { MODEL_BS = 0, MODEL_DUPIRE = 1 };
+enum ProductKind : int { PROD_EUROPEAN = 0, PROD_UOC = 1, PROD_EUROPEANS = 2 };
+enum RngKind : int { RNG_MRG = 0, RNG_SOBOL = 1 };
+
+// Error bits written by kernels into McParams::err (host turns them into CF_E_DEVICE).
+enum DeviceError : int { DEVERR_TMA_TIMEOUT = 1, DEVERR_FIXED_RANGE = 2 };
+
+// Fixed-point accumulation: every sum is held as two int64 words, hi in units of 2^-20 and
+// lo in units of 2^-60.  Integer addition is associative, so sums are bit-identical for any
+// order of the atomic adds (deterministic across launches, grids and streams).
+constexpr int FIX_HI_SHIFT = 20;
+constexpr int FIX_LO_SHIFT = 60;
+constexpr int FIX_CARRY_SHIFT = FIX_LO_SHIFT - FIX_HI_SHIFT;
+
+// Accumulator layout (one hi/lo pair each):
+//   [0, nRisk)                   parameter adjoints (risk mode; 0 in value mode)
+//   [nRisk, nRisk+nPay)          sum of payoff k
+//   [nRisk+nPay, nRisk+2nPay)    sum of payoff k squared
+//   nRisk+2nPay, +1              sum / sum of squares of the aggregate sum_k w_k payoff_k
+struct McParams
+{
+    // sizes
+    long long nPath;
+    int nSteps;      // Gaussians per path (simDim)
+    int nEv;         // product event dates
+    int nPay;
+    int nRisk;       // parameters carried in the accumulators (0 for value runs)
+    int nAcc;
+
+    // random numbers
+    unsigned seed1, seed2;
+    const unsigned* sobolDir;              // [32][nSteps]
+    const unsigned long long* mrgJumpA;    // [64][9] A^(2^k) mod m1
+    const unsigned long long* mrgJumpB;    // [64][9] B^(2^k) mod m2
+
+    // model: Black-Scholes
+    int spotMeasure;
+    double spot, vol;
+    const double* bsD;    // [5][nSteps]: drift, std, dt, sqrt(dt), d drift / d vol
+    const float* bsF;
+    // model: Dupire
+    int nS, nT;
+    double x0d;           // starting state of the FP64 form: log(spot)
+    float s0f;            // FP32 form works in y = x - log(spot), spot = s0f * exp(y)
+    const double* Xd;     // [nS] log spots (FP32 form: shifted by -log(spot))
+    const float* Xf;
+    const double* invdXd; // [nS] 1 / (X[k+1] - X[k])
+    const float* invdXf;
+    const double* Yd;     // [nSteps][nS] local vols pre-interpolated in time, times sqrt(dt)
+    const float* Yf;
+    const int* colA;      // [nSteps] time node of the lower time weight
+    const int* colB;
+    const double* cAd;    // [nSteps] d Y[i][j] / d vol[j][colA] (= sqrt(dt) * (1 - tw))
+    const float* cAf;
+    const double* cBd;    // [nSteps] d Y[i][j] / d vol[j][colB] (0 when flat)
+    const float* cBf;
+    int stageY;           // 1: stage Y into shared memory (cp.async.bulk)
+    // Bucket index of the log-spot grid: bucket b of nBuckets equal slices of [X0, X_last]
+    // holds the upper_bound of its left edge, a starting guess for the interpolation search.
+    int nBuckets;
+    const int* bucket;
+    double bX0d, bInvWd;
+    float bX0f, bInvWf;
+
+    // events
+    const int* evAtStep;  // [nSteps+1] product date index reached at timeline point i, or -1
+    const double* evD;    // [7][nEv]: ff, tauF, disc, tauD, numeraire (factor), t, needNum
+    const float* evF;
+
+    // product
+    int callPut;
+    double strike, barSmooth, minusSmooth, twoSmooth;
+    double logBandD;      // band test threshold in the state variable (FP64 form)
+    float logBandF;       // (FP32 form)
+    const double* kD;     // Europeans strikes, flattened by event
+    const float* kF;
+    const int* evPayOff;  // [nEv+1] payoff offsets per event (Europeans)
+
+    // risk
+    const double* w;      // [nPay] aggregation weights
+    const float* wf;
+
+    // outputs
+    long long* acc;       // [nAcc][2]
+    int* err;
+
+    // per-thread scratch of the reverse sweep, layout [field][step][thread]
+    void* scratch;
+    long long scratchThreads;
+    int scratchFields;
+};
+
+// Kernel configuration chosen by the host.
+struct McLaunch
+{
+    int model, prod, rng, fp32, risk;
+    int grid, block;
+    size_t smem;
+};
+
+int launch_mc(const McLaunch& l, const McParams& p, void* stream);   // returns cudaError_t
+int mc_smem_bytes(const McLaunch& l, const McParams& p, int stageY, size_t* bytes);
+int mc_occupancy(const McLaunch& l, size_t smem, int* blocksPerSM);
+int launch_finalize(const McParams& p, double invN, double* out, void* stream);
+
+}  // namespace cf

@@ -1,0 +1,913 @@
+// Host engine behind the C ABI (include/cfgpu.h): the model / product store, the lowering
+// of a (model, product) pair into flat device tables, and the launch of the Monte Carlo
+// kernels.  Reference interfaces mirrored: store.h (registry), mcBase.h Model/Product
+// (allocate/init/timeline/defline/payoffLabels/parameterLabels), main.h entry points.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/cfgpu.h"
+#include "cf_params.h"
+#include "engine.h"
+#include "host_math.h"
+
+namespace cf {
+
+int launch_sobol_points(const unsigned* dir, int dim, long long first, int n, unsigned* out, void* stream);
+int launch_mrg_state(const unsigned long long* A, const unsigned long long* B, unsigned s1, unsigned s2,
+                     unsigned long long skip, unsigned* out, void* stream);
+int launch_gauss(int sobol, const unsigned* dir, const unsigned long long* A, const unsigned long long* B,
+                 unsigned s1, unsigned s2, int dim, long long first, int n, double* out, void* stream);
+
+thread_local std::string g_lastError;
+
+int fail(int code, const std::string& msg)
+{
+    g_lastError = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what)
+{
+    return fail(e == cudaErrorMemoryAllocation ? CF_E_NOMEM : CF_E_CUDA,
+                std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CF_CUDA(call)                                         \
+    do                                                        \
+    {                                                         \
+        cudaError_t e_ = (call);                              \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call);   \
+    } while (0)
+
+// ------------------------------------------------------------------------------------
+// Device buffers
+// ------------------------------------------------------------------------------------
+int DevBuf::ensure(size_t n)
+{
+    if (n <= bytes) return CF_OK;
+    release();
+    const size_t want = n + n / 4;
+    cudaError_t e = cudaMalloc(&ptr, want);
+    if (e != cudaSuccess)
+    {
+        ptr = nullptr;
+        bytes = 0;
+        return cuda_fail(e, "cudaMalloc");
+    }
+    bytes = want;
+    return CF_OK;
+}
+
+void DevBuf::release()
+{
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    bytes = 0;
+}
+
+// ------------------------------------------------------------------------------------
+// Products: timelines, deflines and labels (mcPrd.h:43-80, 149-211, 305-340).
+// ------------------------------------------------------------------------------------
+void ProductDesc::build()
+{
+    timeline.clear();
+    fwdMat.clear();
+    discMat.clear();
+    needNum.clear();
+    labels.clear();
+    kflat.clear();
+    payOff.clear();
+    if (kind == PROD_EUROPEAN)
+    {
+        timeline = {exercise};
+        fwdMat = {settlement};
+        discMat = {settlement};
+        needNum = {1};
+        labels = {settlement == exercise ? "call " + fmt2(strike) + " " + fmt2(exercise)
+                                         : "call " + fmt2(strike) + " " + fmt2(exercise) + " " + fmt2(settlement)};
+    }
+    else if (kind == PROD_UOC)
+    {
+        timeline.push_back(0.0);
+        double t = freq;
+        while (maturity - t > kOneHour)
+        {
+            timeline.push_back(t);
+            t += freq;
+        }
+        timeline.push_back(maturity);
+        for (double x : timeline)
+        {
+            fwdMat.push_back(x);
+            discMat.push_back(NAN);
+            needNum.push_back(0);
+        }
+        needNum.back() = 1;
+        const std::string l1 = std::string(callPut ? "put " : "call ") + fmt2(maturity) + " " + fmt2(strike);
+        labels = {l1 + " up and out " + fmt2(barrier) + " monitoring freq " + fmt2(freq) + " smooth " + fmt2(smooth),
+                  l1};
+    }
+    else
+    {
+        std::map<double, std::vector<double>> opts;
+        for (size_t i = 0; i < mats.size(); ++i) opts[mats[i]].push_back(strikes[i]);
+        for (auto& kv : opts)
+        {
+            timeline.push_back(kv.first);
+            fwdMat.push_back(kv.first);
+            discMat.push_back(NAN);
+            needNum.push_back(1);
+            payOff.push_back(int(kflat.size()));
+            for (double k : kv.second)
+            {
+                kflat.push_back(k);
+                labels.push_back("call " + fmt2(kv.first) + " " + fmt2(k));
+            }
+        }
+        payOff.push_back(int(kflat.size()));
+    }
+}
+
+void ModelDesc::build()
+{
+    labels.clear();
+    labels.push_back("spot");
+    if (kind == MODEL_BS)
+    {
+        labels.push_back("vol");
+        labels.push_back("rate");
+        labels.push_back("div");
+    }
+    else
+        for (size_t i = 0; i < spots.size(); ++i)
+            for (size_t j = 0; j < times.size(); ++j)
+                labels.push_back("lvol " + fmt2(spots[i]) + " " + fmt2(times[j]));
+}
+
+int ModelDesc::numParams() const { return kind == MODEL_BS ? 4 : 1 + int(spots.size() * times.size()); }
+
+// ------------------------------------------------------------------------------------
+// Plan: the flat device tables of one (model, product) pair.
+// ------------------------------------------------------------------------------------
+namespace {
+
+struct Packer
+{
+    std::vector<unsigned char> buf;
+    size_t put(const void* p, size_t n)
+    {
+        const size_t off = (buf.size() + 255) & ~size_t(255);
+        buf.resize(off + ((n + 15) & ~size_t(15)), 0);
+        if (n) std::memcpy(buf.data() + off, p, n);
+        return off;
+    }
+    template <class T>
+    size_t vec(const std::vector<T>& v) { return put(v.data(), v.size() * sizeof(T)); }
+};
+
+template <class T>
+std::vector<float> to_f(const std::vector<T>& v)
+{
+    return std::vector<float>(v.begin(), v.end());
+}
+
+}  // namespace
+
+int Context::buildPlan(const ModelDesc& m, const ProductDesc& pd, Plan& plan)
+{
+    // plan arrives freshly constructed (getPlan makes a new one per build)
+    plan.model = m.kind;
+    plan.prod = pd.kind;
+    plan.nPay = int(pd.labels.size());
+    plan.nParam = m.numParams();
+    plan.nEv = int(pd.timeline.size());
+    McParams& P = plan.base;
+    std::memset(&P, 0, sizeof(P));
+    P.nEv = plan.nEv;
+    P.nPay = plan.nPay;
+    P.spot = m.spot;
+    P.vol = m.vol;
+    P.spotMeasure = m.qSpot ? 1 : 0;
+    P.callPut = pd.callPut;
+    P.strike = pd.strike;
+
+    Packer pk;
+    std::vector<double> tl;
+    std::vector<int> evAtStep;
+    std::vector<double> ev(7 * size_t(plan.nEv), 0.0);
+    double frontSpot = m.spot;
+    size_t oBs = 0, oX = 0, oInv = 0, oY = 0, oXf = 0, oInvf = 0, oYf = 0, oCA = 0, oCB = 0, oCAf = 0, oCBf = 0,
+           oColA = 0, oColB = 0, oBsF = 0, oBucket = 0;
+
+    if (m.kind == MODEL_BS)
+    {
+        // mcMdlBS.h:149-277: timeline = today + product dates after today.
+        tl.push_back(0.0);
+        for (double t : pd.timeline)
+            if (t > 0.0) tl.push_back(t);
+        const bool todayOn = pd.timeline[0] == 0.0;
+        const int n = int(tl.size()) - 1;
+        evAtStep.assign(n + 1, -1);
+        if (todayOn) evAtStep[0] = 0;
+        for (int i = 1; i <= n; ++i) evAtStep[i] = todayOn ? i : i - 1;
+        const double mu = m.rate - m.div;
+        std::vector<double> bsd(5 * size_t(n));
+        for (int i = 0; i < n; ++i)
+        {
+            const double dt = tl[i + 1] - tl[i];
+            bsd[i] = m.qSpot ? (mu + 0.5 * m.vol * m.vol) * dt : (mu - 0.5 * m.vol * m.vol) * dt;
+            bsd[n + i] = m.vol * std::sqrt(dt);
+            bsd[2 * n + i] = dt;
+            bsd[3 * n + i] = std::sqrt(dt);
+            bsd[4 * n + i] = (m.qSpot ? m.vol : -m.vol) * dt;
+        }
+        for (int e = 0; e < plan.nEv; ++e)
+        {
+            const double t = pd.timeline[e];
+            ev[e] = std::exp(mu * (pd.fwdMat[e] - t));
+            ev[plan.nEv + e] = pd.fwdMat[e] - t;
+            const bool hasD = !std::isnan(pd.discMat[e]);
+            ev[2 * plan.nEv + e] = hasD ? std::exp(-m.rate * (pd.discMat[e] - t)) : 1.0;
+            ev[3 * plan.nEv + e] = hasD ? pd.discMat[e] - t : 0.0;
+            ev[4 * plan.nEv + e] = m.qSpot ? std::exp(m.div * t) / m.spot : std::exp(m.rate * t);
+            ev[5 * plan.nEv + e] = t;
+            ev[6 * plan.nEv + e] = pd.needNum[e] ? 1.0 : 0.0;
+        }
+        frontSpot = m.spot * ev[0];  // path.front() forward of the first product date
+        oBs = pk.vec(bsd);
+        oBsF = pk.vec(to_f(bsd));
+        plan.nSteps = n;
+    }
+    else
+    {
+        // mcMdlDupire.h:165-217: refined timeline, event flags, vols pre-interpolated in time.
+        tl = fill_data(pd.timeline, m.maxDt, kHalfDay, {0.0});
+        const int n = int(tl.size()) - 1;
+        if (n < 1) return fail(CF_E_SHAPE, "Dupire: empty simulation timeline");
+        evAtStep.assign(n + 1, -1);
+        int e = 0;
+        for (int i = 0; i <= n; ++i)
+            if (std::binary_search(pd.timeline.begin(), pd.timeline.end(), tl[i])) evAtStep[i] = e++;
+        if (e != plan.nEv) return fail(CF_E_SHAPE, "Dupire: product dates before today are not supported");
+        const int nS = int(m.spots.size()), nT = int(m.times.size());
+        std::vector<double> X(nS), inv(nS, 0.0), Y(size_t(n) * nS), cAv(n), cBv(n);
+        std::vector<int> colA(n), colB(n);
+        for (int j = 0; j < nS; ++j) X[j] = std::log(m.spots[j]);
+        for (int j = 0; j + 1 < nS; ++j) inv[j] = 1.0 / (X[j + 1] - X[j]);
+        std::vector<double> row(nT);
+        for (int i = 0; i < n; ++i)
+        {
+            const double sq = std::sqrt(tl[i + 1] - tl[i]);
+            for (int j = 0; j < nS; ++j)
+                Y[size_t(i) * nS + j] = sq * interp_lin(m.times.data(), nT, &m.vols[size_t(j) * nT], tl[i]);
+            const double* it = std::upper_bound(m.times.data(), m.times.data() + nT, tl[i]);
+            if (it == m.times.data() + nT || it == m.times.data())
+            {
+                colA[i] = colB[i] = it == m.times.data() ? 0 : nT - 1;
+                cAv[i] = sq;
+                cBv[i] = 0.0;
+            }
+            else
+            {
+                const int k = int(it - m.times.data()) - 1;
+                const double t = (tl[i] - m.times[k]) / (m.times[k + 1] - m.times[k]);
+                colA[i] = k;
+                colB[i] = k + 1;
+                cAv[i] = sq * (1.0 - t);
+                cBv[i] = sq * t;
+            }
+        }
+        const double x0 = std::log(m.spot);
+        std::vector<float> Xf(nS);
+        for (int j = 0; j < nS; ++j) Xf[j] = float(X[j] - x0);
+        P.x0d = x0;
+        P.s0f = float(std::exp(x0));
+        frontSpot = std::exp(x0);  // path.front() spot when today is a product date
+        P.nS = nS;
+        P.nT = nT;
+        // bucket index of the grid (a search hint; the kernel corrects it exactly)
+        const int nB = 512;
+        std::vector<int> bucket(nB, 0);
+        const double w = nS > 1 ? (X[nS - 1] - X[0]) / nB : 1.0;
+        for (int b = 0; b < nB; ++b)
+            bucket[b] = int(std::upper_bound(X.begin(), X.end(), X[0] + b * w) - X.begin());
+        P.nBuckets = nB;
+        P.bX0d = X[0];
+        P.bInvWd = 1.0 / w;
+        P.bX0f = Xf[0];
+        P.bInvWf = float(1.0 / w);
+        oBucket = pk.vec(bucket);
+        oX = pk.vec(X);
+        oInv = pk.vec(inv);
+        oY = pk.vec(Y);
+        oXf = pk.vec(Xf);
+        oInvf = pk.vec(to_f(inv));
+        oYf = pk.vec(to_f(Y));
+        oColA = pk.vec(colA);
+        oColB = pk.vec(colB);
+        oCA = pk.vec(cAv);
+        oCB = pk.vec(cBv);
+        oCAf = pk.vec(to_f(cAv));
+        oCBf = pk.vec(to_f(cBv));
+        plan.nSteps = n;
+        plan.yBytesD = Y.size() * 8;
+        plan.yBytesF = Y.size() * 4;
+    }
+    P.nSteps = plan.nSteps;
+    plan.timeline = tl;
+
+    // product constants (mcPrd.h:235-288: smoothing from the first sample's spot)
+    if (pd.kind == PROD_UOC)
+    {
+        const double smooth = frontSpot * pd.smooth;
+        P.twoSmooth = 2 * smooth;
+        P.barSmooth = pd.barrier + smooth;
+        P.minusSmooth = pd.barrier - smooth;
+        const double lb = P.minusSmooth > 0 ? std::log(P.minusSmooth) : -INFINITY;
+        P.logBandD = lb - 1e-9;
+        P.logBandF = float(m.kind == MODEL_DUPIRE ? lb - P.x0d - 1e-5 : lb - 1e-5);
+    }
+
+    const size_t oEv = pk.vec(evAtStep);
+    const size_t oEvD = pk.vec(ev), oEvF = pk.vec(to_f(ev));
+    std::vector<double> kf = pd.kflat;
+    if (kf.empty()) kf.push_back(0.0);
+    std::vector<int> po = pd.payOff;
+    if (po.empty()) po = {0, 0};
+    const size_t oK = pk.vec(kf), oKf = pk.vec(to_f(kf)), oPo = pk.vec(po);
+    size_t oDir = 0;
+    if (plan.nSteps <= sobol_max_dim()) oDir = pk.vec(sobol_dirs(plan.nSteps));
+    plan.sobolOk = plan.nSteps <= sobol_max_dim();
+
+    int rc = plan.tables.ensure(pk.buf.size());
+    if (rc) return rc;
+    CF_CUDA(cudaMemcpyAsync(plan.tables.ptr, pk.buf.data(), pk.buf.size(), cudaMemcpyHostToDevice, stream));
+    h2d += pk.buf.size();
+    unsigned char* d = static_cast<unsigned char*>(plan.tables.ptr);
+    auto D = [&](size_t off) { return static_cast<const void*>(d + off); };
+    if (m.kind == MODEL_BS)
+    {
+        P.bsD = (const double*)D(oBs);
+        P.bsF = (const float*)D(oBsF);
+    }
+    else
+    {
+        P.Xd = (const double*)D(oX);
+        P.invdXd = (const double*)D(oInv);
+        P.Yd = (const double*)D(oY);
+        P.Xf = (const float*)D(oXf);
+        P.invdXf = (const float*)D(oInvf);
+        P.Yf = (const float*)D(oYf);
+        P.colA = (const int*)D(oColA);
+        P.bucket = (const int*)D(oBucket);
+        P.colB = (const int*)D(oColB);
+        P.cAd = (const double*)D(oCA);
+        P.cBd = (const double*)D(oCB);
+        P.cAf = (const float*)D(oCAf);
+        P.cBf = (const float*)D(oCBf);
+    }
+    P.evAtStep = (const int*)D(oEv);
+    P.evD = (const double*)D(oEvD);
+    P.evF = (const float*)D(oEvF);
+    P.kD = (const double*)D(oK);
+    P.kF = (const float*)D(oKf);
+    P.evPayOff = (const int*)D(oPo);
+    P.sobolDir = plan.sobolOk ? (const unsigned*)D(oDir) : nullptr;
+    plan.evAtStep = evAtStep;
+    return CF_OK;
+}
+
+// ------------------------------------------------------------------------------------
+// Context
+// ------------------------------------------------------------------------------------
+int Context::init(int dev)
+{
+    device = dev;
+    CF_CUDA(cudaSetDevice(dev));
+    CF_CUDA(cudaStreamCreateWithFlags(&ownStream, cudaStreamNonBlocking));
+    stream = ownStream;
+    CF_CUDA(cudaDeviceGetAttribute(&numSMs, cudaDevAttrMultiProcessorCount, dev));
+    uint64_t A[64][9], B[64][9];
+    mrg_jump_tables(A, B);
+    int rc = jump.ensure(sizeof(A) + sizeof(B));
+    if (rc) return rc;
+    CF_CUDA(cudaMemcpy(jump.ptr, A, sizeof(A), cudaMemcpyHostToDevice));
+    CF_CUDA(cudaMemcpy(static_cast<char*>(jump.ptr) + sizeof(A), B, sizeof(B), cudaMemcpyHostToDevice));
+    jumpA = static_cast<const unsigned long long*>(jump.ptr);
+    jumpB = jumpA + 64 * 9;
+    if ((rc = err.ensure(16))) return rc;
+    return CF_OK;
+}
+
+Context::~Context()
+{
+    cudaSetDevice(device);
+    plans.clear();
+    if (ownStream) cudaStreamDestroy(ownStream);
+}
+
+int Context::getPlan(const std::string& mid, const std::string& pid, Plan*& out)
+{
+    auto mi = models.find(mid);
+    auto pi = products.find(pid);
+    if (mi == models.end() || pi == products.end())
+        return fail(CF_E_NOTFOUND, "Could not retrieve model and product: '" + mid + "', '" + pid + "'");
+    auto key = std::make_pair(mid, pid);
+    auto it = plans.find(key);
+    if (it != plans.end() && it->second->mver == mi->second.version && it->second->pver == pi->second.version)
+    {
+        out = it->second.get();
+        return CF_OK;
+    }
+    auto plan = std::make_unique<Plan>();
+    int rc = buildPlan(mi->second, pi->second, *plan);
+    if (rc) return rc;
+    plan->mver = mi->second.version;
+    plan->pver = pi->second.version;
+    out = plan.get();
+    plans[key] = std::move(plan);
+    return CF_OK;
+}
+
+// Enqueue one value (risk = false) or risk (risk = true, weights[nPay]) run.
+int Context::enqueue(Plan& plan, const cf_num_param& num, bool risk, const double* weights)
+{
+    if (num.numPath <= 0) return fail(CF_E_ARG, "numPath must be positive");
+    const bool sobol = num.useSobol != 0;
+    if (sobol && !plan.sobolOk)
+        return fail(CF_E_SHAPE, "Sobol dimension " + std::to_string(plan.nSteps) + " exceeds the " +
+                                    std::to_string(sobol_max_dim()) + " dimensions of the direction numbers");
+    const bool fp32 = num.precision == CF_FP32;
+    McParams p = plan.base;
+    p.nPath = num.numPath;
+    p.seed1 = unsigned(num.seed1);
+    p.seed2 = unsigned(num.seed2);
+    p.mrgJumpA = jumpA;
+    p.mrgJumpB = jumpB;
+    p.nRisk = risk ? plan.nParam : 0;
+    p.nAcc = p.nRisk + 2 * plan.nPay + 2;
+    // weights (double and float copies) and accumulators share one buffer
+    const size_t wBytes = ((size_t(plan.nPay) * 12 + 255) & ~size_t(255));
+    const size_t accBytes = size_t(p.nAcc) * 16;
+    int rc = work.ensure(wBytes + accBytes);
+    if (rc) return rc;
+    hostW.assign(size_t(plan.nPay) * 3, 0);
+    std::vector<double> wd(plan.nPay, 0.0);
+    std::vector<float> wf(plan.nPay, 0.0f);
+    if (weights)
+        for (int k = 0; k < plan.nPay; ++k)
+        {
+            wd[k] = weights[k];
+            wf[k] = float(weights[k]);
+        }
+    char* wbase = static_cast<char*>(work.ptr);
+    CF_CUDA(cudaMemcpyAsync(wbase, wd.data(), wd.size() * 8, cudaMemcpyHostToDevice, stream));
+    CF_CUDA(cudaMemcpyAsync(wbase + size_t(plan.nPay) * 8, wf.data(), wf.size() * 4, cudaMemcpyHostToDevice,
+                            stream));
+    h2d += wd.size() * 12;
+    p.w = reinterpret_cast<const double*>(wbase);
+    p.wf = reinterpret_cast<const float*>(wbase + size_t(plan.nPay) * 8);
+    p.acc = reinterpret_cast<long long*>(wbase + wBytes);
+    p.err = static_cast<int*>(err.ptr);
+    CF_CUDA(cudaMemsetAsync(p.acc, 0, accBytes, stream));
+    CF_CUDA(cudaMemsetAsync(p.err, 0, 4, stream));
+
+    McLaunch l{plan.model, plan.prod, sobol ? RNG_SOBOL : RNG_MRG, fp32 ? 1 : 0, risk ? 1 : 0, 0, 0, 0};
+    // Shared-memory staging of the interpolated local vols (a bulk copy through the TMA
+    // unit): used only when it costs no occupancy; otherwise the table is read through L1.
+    int stage = 0;
+    size_t smem0 = 0, smem1 = 0;
+    mc_smem_bytes(l, p, 0, &smem0);
+    int occ0 = 0, occ1 = 0;
+    rc = mc_occupancy(l, smem0, &occ0);
+    if (rc) return cuda_fail(cudaError_t(rc), "occupancy");
+    if (plan.model == MODEL_DUPIRE)
+    {
+        mc_smem_bytes(l, p, 1, &smem1);
+        const char* env = std::getenv("CF_STAGE_Y");
+        if (smem1 <= 200 * 1024)
+        {
+            rc = mc_occupancy(l, smem1, &occ1);
+            if (rc) return cuda_fail(cudaError_t(rc), "occupancy");
+            stage = occ1 >= occ0;  // only when it costs no occupancy (the kernel is latency-bound)
+        }
+        if (env && env[0] == '0') stage = 0;
+        if (env && env[0] == '1' && occ1 > 0) stage = 1;
+    }
+    p.stageY = stage;
+    l.smem = stage ? smem1 : smem0;
+    const int occ = stage ? occ1 : occ0;
+    if (occ < 1) return fail(CF_E_SHAPE, "kernel does not fit on an SM (shared memory " + std::to_string(l.smem) + ")");
+    const long long threadsNeeded = sobol ? (p.nPath / 32 + 1) * 32 : (p.nPath + 1) / 2;
+    long long grid = (threadsNeeded + 127) / 128;
+    const long long maxGrid = (long long)numSMs * occ;
+    if (grid > maxGrid) grid = maxGrid;
+    if (grid < 1) grid = 1;
+    l.grid = int(grid);
+    l.block = 128;
+    if (risk)
+    {
+        const int NP = sobol ? 1 : 2;
+        p.scratchFields = 1 + NP + (plan.prod == PROD_UOC ? NP : 0);
+        // kernels index the scratch with 32-bit offsets: keep fields*(steps+1)*threads < 2^31
+        const long long perThread = (long long)p.scratchFields * (plan.nSteps + 1);
+        const long long maxThreads = ((1LL << 31) - 1) / perThread;
+        if (grid * 128 > maxThreads) grid = std::max(1LL, maxThreads / 128);
+        l.grid = int(grid);
+        p.scratchThreads = grid * 128;
+        const size_t bytes = size_t(p.scratchFields) * size_t(plan.nSteps + 1) * size_t(p.scratchThreads) *
+                             (fp32 ? 4 : 8);
+        if ((rc = scratch.ensure(bytes))) return rc;
+        p.scratch = scratch.ptr;
+    }
+    rc = launch_mc(l, p, stream);
+    if (rc) return cuda_fail(cudaError_t(rc), "mc_kernel launch");
+    last = p;
+    lastLaunch = l;
+    lastPlan = &plan;
+    lastRisk = risk;
+    launches = 1;
+    return CF_OK;
+}
+
+int Context::fetch(double* values, double* stderrs, double* aggregate, double* risks)
+{
+    if (!lastPlan) return fail(CF_E_ARG, "nothing enqueued");
+    const McParams& p = last;
+    std::vector<long long> acc(size_t(p.nAcc) * 2);
+    int e = 0;
+    CF_CUDA(cudaMemcpyAsync(acc.data(), p.acc, acc.size() * 8, cudaMemcpyDeviceToHost, stream));
+    CF_CUDA(cudaMemcpyAsync(&e, p.err, 4, cudaMemcpyDeviceToHost, stream));
+    CF_CUDA(cudaStreamSynchronize(stream));
+    d2h += acc.size() * 8 + 4;
+    if (e) return fail(CF_E_DEVICE, "kernel error flag " + std::to_string(e));
+    const double n = double(p.nPath);
+    auto val = [&](int i) { return fix_value_host(acc[2 * size_t(i)], acc[2 * size_t(i) + 1]); };
+    for (int k = 0; k < p.nPay; ++k)
+    {
+        const double s = val(p.nRisk + k), q = val(p.nRisk + p.nPay + k);
+        const double mean = s / n;
+        if (values) values[k] = mean;
+        if (stderrs) stderrs[k] = std::sqrt(std::max(0.0, q / n - mean * mean) / n);
+    }
+    if (aggregate) aggregate[0] = val(p.nRisk + 2 * p.nPay) / n;
+    if (aggregate && stderrs == nullptr) {}
+    if (risks && lastRisk)
+        for (int j = 0; j < p.nRisk; ++j) risks[j] = val(j) / n;
+    return CF_OK;
+}
+
+double fix_value_host(long long hi, long long lo)
+{
+    return (double)hi * (1.0 / 1048576.0) + (double)lo * (1.0 / 1152921504606846976.0);
+}
+
+}  // namespace cf
+
+// =====================================================================================
+// C ABI
+// =====================================================================================
+using namespace cf;
+
+#define CF_CTX()                                               \
+    if (!ctx) return fail(CF_E_ARG, "null context");           \
+    std::lock_guard<std::mutex> lock_(ctx->mu);                \
+    cudaSetDevice(ctx->c.device);
+
+extern "C" {
+
+int cf_create(int device, cf_context** out)
+{
+    if (!out) return fail(CF_E_ARG, "null output");
+    *out = nullptr;
+    auto c = std::make_unique<cf_context>();
+    const int rc = c->c.init(device);
+    if (rc) return rc;
+    *out = c.release();
+    return CF_OK;
+}
+
+int cf_destroy(cf_context* ctx)
+{
+    delete ctx;
+    return CF_OK;
+}
+
+int cf_last_error(char* buf, size_t size)
+{
+    if (!buf || !size) return CF_E_ARG;
+    std::snprintf(buf, size, "%s", g_lastError.c_str());
+    return CF_OK;
+}
+
+int cf_set_stream(cf_context* ctx, void* stream)
+{
+    CF_CTX();
+    ctx->c.stream = stream ? static_cast<cudaStream_t>(stream) : ctx->c.ownStream;
+    return CF_OK;
+}
+
+int cf_transfer_stats(cf_context* ctx, uint64_t* h2dBytes, uint64_t* d2hBytes)
+{
+    CF_CTX();
+    if (h2dBytes) *h2dBytes = ctx->c.h2d;
+    if (d2hBytes) *d2hBytes = ctx->c.d2h;
+    return CF_OK;
+}
+
+int cf_synchronize(cf_context* ctx)
+{
+    CF_CTX();
+    CF_CUDA(cudaStreamSynchronize(ctx->c.stream));
+    return CF_OK;
+}
+
+static int check_id(const char* id) { return id && *id ? CF_OK : fail(CF_E_ARG, "empty id"); }
+
+int cf_put_black_scholes(cf_context* ctx, double spot, double vol, int qSpot, double rate, double div, const char* id)
+{
+    CF_CTX();
+    if (check_id(id)) return CF_E_ARG;
+    ModelDesc m;
+    m.kind = MODEL_BS;
+    m.spot = spot;
+    m.vol = vol;
+    m.qSpot = qSpot != 0;
+    m.rate = rate;
+    m.div = div;
+    m.version = ++ctx->c.versionCounter;
+    m.build();
+    ctx->c.models[id] = std::move(m);
+    return CF_OK;
+}
+
+int cf_put_dupire(cf_context* ctx, double spot, const double* spots, int nSpots, const double* times, int nTimes,
+                  const double* vols, double maxDt, const char* id)
+{
+    CF_CTX();
+    if (check_id(id)) return CF_E_ARG;
+    if (!spots || !times || !vols || nSpots < 1 || nTimes < 1 || !(maxDt > 0))
+        return fail(CF_E_ARG, "putDupire: bad grid");
+    ModelDesc m;
+    m.kind = MODEL_DUPIRE;
+    m.spot = spot;
+    m.spots.assign(spots, spots + nSpots);
+    m.times.assign(times, times + nTimes);
+    m.vols.assign(vols, vols + size_t(nSpots) * nTimes);
+    m.maxDt = maxDt;
+    m.version = ++ctx->c.versionCounter;
+    m.build();
+    ctx->c.models[id] = std::move(m);
+    return CF_OK;
+}
+
+int cf_put_european(cf_context* ctx, double strike, double exerciseDate, double settlementDate, const char* id)
+{
+    CF_CTX();
+    if (check_id(id)) return CF_E_ARG;
+    ProductDesc p;
+    p.kind = PROD_EUROPEAN;
+    p.strike = strike;
+    p.exercise = exerciseDate;
+    p.settlement = settlementDate;
+    p.version = ++ctx->c.versionCounter;
+    p.build();
+    ctx->c.products[id] = std::move(p);
+    return CF_OK;
+}
+
+int cf_put_barrier(cf_context* ctx, double strike, double barrier, double maturity, double monitorFreq,
+                   double smooth, int callPut, const char* id)
+{
+    CF_CTX();
+    if (check_id(id)) return CF_E_ARG;
+    if (!(monitorFreq > 0) || !(maturity > 0)) return fail(CF_E_ARG, "putBarrier: bad maturity or frequency");
+    ProductDesc p;
+    p.kind = PROD_UOC;
+    p.strike = strike;
+    p.barrier = barrier;
+    p.maturity = maturity;
+    p.freq = monitorFreq;
+    p.smooth = smooth <= 0 ? kEps : smooth;  // store.h:153
+    p.callPut = callPut ? 1 : 0;
+    p.version = ++ctx->c.versionCounter;
+    p.build();
+    ctx->c.products[id] = std::move(p);
+    return CF_OK;
+}
+
+int cf_put_europeans(cf_context* ctx, const double* maturities, const double* strikes, int n, const char* id)
+{
+    CF_CTX();
+    if (check_id(id)) return CF_E_ARG;
+    if (!maturities || !strikes || n < 1) return fail(CF_E_ARG, "putEuropeans: empty portfolio");
+    ProductDesc p;
+    p.kind = PROD_EUROPEANS;
+    p.mats.assign(maturities, maturities + n);
+    p.strikes.assign(strikes, strikes + n);
+    p.version = ++ctx->c.versionCounter;
+    p.build();
+    ctx->c.products[id] = std::move(p);
+    return CF_OK;
+}
+
+static int write_labels(const std::vector<std::string>& l, char* buf, size_t size, int* count, size_t* needed)
+{
+    std::string s;
+    for (size_t i = 0; i < l.size(); ++i)
+    {
+        if (i) s += '\n';
+        s += l[i];
+    }
+    if (count) *count = int(l.size());
+    if (needed) *needed = s.size() + 1;
+    if (!buf) return CF_OK;
+    if (size < s.size() + 1) return fail(CF_E_SHAPE, "label buffer too small");
+    std::memcpy(buf, s.c_str(), s.size() + 1);
+    return CF_OK;
+}
+
+int cf_payoff_labels(cf_context* ctx, const char* productId, char* buf, size_t size, int* count, size_t* needed)
+{
+    CF_CTX();
+    auto it = ctx->c.products.find(productId ? productId : "");
+    if (it == ctx->c.products.end()) return fail(CF_E_NOTFOUND, "product not found");
+    return write_labels(it->second.labels, buf, size, count, needed);
+}
+
+int cf_parameter_labels(cf_context* ctx, const char* modelId, char* buf, size_t size, int* count, size_t* needed)
+{
+    CF_CTX();
+    auto it = ctx->c.models.find(modelId ? modelId : "");
+    if (it == ctx->c.models.end()) return fail(CF_E_NOTFOUND, "model not found");
+    return write_labels(it->second.labels, buf, size, count, needed);
+}
+
+int cf_shapes(cf_context* ctx, const char* modelId, const char* productId, int* nPay, int* nParam, int* simDim)
+{
+    CF_CTX();
+    Plan* plan;
+    int rc = ctx->c.getPlan(modelId ? modelId : "", productId ? productId : "", plan);
+    if (rc) return rc;
+    if (nPay) *nPay = plan->nPay;
+    if (nParam) *nParam = plan->nParam;
+    if (simDim) *simDim = plan->nSteps;
+    return CF_OK;
+}
+
+int cf_value(cf_context* ctx, const char* modelId, const char* productId, const cf_num_param* num, double* values,
+             double* stderrs)
+{
+    CF_CTX();
+    if (!num || !values) return fail(CF_E_ARG, "null argument");
+    Plan* plan;
+    int rc = ctx->c.getPlan(modelId ? modelId : "", productId ? productId : "", plan);
+    if (rc) return rc;
+    if ((rc = ctx->c.enqueue(*plan, *num, false, nullptr))) return rc;
+    return ctx->c.fetch(values, stderrs, nullptr, nullptr);
+}
+
+static int payoff_index(const Plan& plan, const ProductDesc& pd, const char* label, int* idx)
+{
+    *idx = 0;
+    if (!label || !*label) return CF_OK;
+    for (size_t i = 0; i < pd.labels.size(); ++i)
+        if (pd.labels[i] == label)
+        {
+            *idx = int(i);
+            return CF_OK;
+        }
+    (void)plan;
+    return fail(CF_E_NOTFOUND, "AADriskOne() : payoff not found");
+}
+
+int cf_aad_risk_one(cf_context* ctx, const char* modelId, const char* productId, const cf_num_param* num,
+                    const char* riskPayoff, double* payoffValues, double* riskPayoffValue, double* risks)
+{
+    CF_CTX();
+    if (!num || !risks) return fail(CF_E_ARG, "null argument");
+    Plan* plan;
+    int rc = ctx->c.getPlan(modelId ? modelId : "", productId ? productId : "", plan);
+    if (rc) return rc;
+    int k;
+    if ((rc = payoff_index(*plan, ctx->c.products[productId], riskPayoff, &k))) return rc;
+    std::vector<double> w(plan->nPay, 0.0);
+    w[k] = 1.0;
+    if ((rc = ctx->c.enqueue(*plan, *num, true, w.data()))) return rc;
+    return ctx->c.fetch(payoffValues, nullptr, riskPayoffValue, risks);
+}
+
+int cf_aad_risk_aggregate(cf_context* ctx, const char* modelId, const char* productId, const double* notionals,
+                          const cf_num_param* num, double* payoffValues, double* aggregateValue, double* risks)
+{
+    CF_CTX();
+    if (!num || !risks || !notionals) return fail(CF_E_ARG, "null argument");
+    Plan* plan;
+    int rc = ctx->c.getPlan(modelId ? modelId : "", productId ? productId : "", plan);
+    if (rc) return rc;
+    if ((rc = ctx->c.enqueue(*plan, *num, true, notionals))) return rc;
+    return ctx->c.fetch(payoffValues, nullptr, aggregateValue, risks);
+}
+
+int cf_aad_risk_multi(cf_context* ctx, const char* modelId, const char* productId, const cf_num_param* num,
+                      double* values, double* risks)
+{
+    CF_CTX();
+    if (!num || !risks) return fail(CF_E_ARG, "null argument");
+    Plan* plan;
+    int rc = ctx->c.getPlan(modelId ? modelId : "", productId ? productId : "", plan);
+    if (rc) return rc;
+    return ctx->c.riskMulti(*plan, *num, values, risks);
+}
+
+int cf_enqueue(cf_context* ctx, const char* modelId, const char* productId, const cf_num_param* num, int risk,
+               const double* weights, int* launches)
+{
+    CF_CTX();
+    if (!num) return fail(CF_E_ARG, "null argument");
+    Plan* plan;
+    int rc = ctx->c.getPlan(modelId ? modelId : "", productId ? productId : "", plan);
+    if (rc) return rc;
+    std::vector<double> w;
+    if (risk && !weights)
+    {
+        w.assign(plan->nPay, 0.0);
+        w[0] = 1.0;
+        weights = w.data();
+    }
+    if ((rc = ctx->c.enqueue(*plan, *num, risk != 0, weights))) return rc;
+    if (launches) *launches = ctx->c.launches;
+    return CF_OK;
+}
+
+int cf_fetch_result(cf_context* ctx, double* values, double* stderrs, double* aggregate, double* risks)
+{
+    CF_CTX();
+    return ctx->c.fetch(values, stderrs, aggregate, risks);
+}
+
+int cf_sobol_points(cf_context* ctx, int dim, int64_t firstPath, int nPaths, uint32_t* out)
+{
+    CF_CTX();
+    if (dim < 1 || dim > sobol_max_dim() || nPaths < 0 || firstPath < 0 || !out)
+        return fail(CF_E_ARG, "sobol: bad dimension or range");
+    const auto dirs = sobol_dirs(dim);
+    DevBuf d, o;
+    int rc;
+    if ((rc = d.ensure(dirs.size() * 4)) || (rc = o.ensure(size_t(nPaths) * dim * 4 + 4))) return rc;
+    CF_CUDA(cudaMemcpyAsync(d.ptr, dirs.data(), dirs.size() * 4, cudaMemcpyHostToDevice, ctx->c.stream));
+    rc = launch_sobol_points((const unsigned*)d.ptr, dim, firstPath, nPaths, (unsigned*)o.ptr, ctx->c.stream);
+    if (rc) return cuda_fail(cudaError_t(rc), "sobol_points");
+    CF_CUDA(cudaMemcpyAsync(out, o.ptr, size_t(nPaths) * dim * 4, cudaMemcpyDeviceToHost, ctx->c.stream));
+    CF_CUDA(cudaStreamSynchronize(ctx->c.stream));
+    d.release();
+    o.release();
+    return CF_OK;
+}
+
+int cf_mrg_state(cf_context* ctx, unsigned seed1, unsigned seed2, int dim, int64_t firstPath, uint32_t* state6)
+{
+    CF_CTX();
+    if (dim < 1 || firstPath < 0 || !state6) return fail(CF_E_ARG, "mrg: bad argument");
+    DevBuf o;
+    int rc;
+    if ((rc = o.ensure(32))) return rc;
+    rc = launch_mrg_state(ctx->c.jumpA, ctx->c.jumpB, seed1, seed2, (unsigned long long)(firstPath / 2) * dim,
+                          (unsigned*)o.ptr, ctx->c.stream);
+    if (rc) return cuda_fail(cudaError_t(rc), "mrg_state");
+    CF_CUDA(cudaMemcpyAsync(state6, o.ptr, 24, cudaMemcpyDeviceToHost, ctx->c.stream));
+    CF_CUDA(cudaStreamSynchronize(ctx->c.stream));
+    o.release();
+    return CF_OK;
+}
+
+int cf_gaussians(cf_context* ctx, int useSobol, unsigned seed1, unsigned seed2, int dim, int64_t firstPath, int nPaths,
+                 double* out)
+{
+    CF_CTX();
+    if (dim < 1 || nPaths < 0 || firstPath < 0 || !out || (useSobol && dim > sobol_max_dim()))
+        return fail(CF_E_ARG, "gaussians: bad argument");
+    DevBuf d, o;
+    int rc;
+    std::vector<uint32_t> dirs = useSobol ? sobol_dirs(dim) : std::vector<uint32_t>(1);
+    if ((rc = d.ensure(dirs.size() * 4)) || (rc = o.ensure(size_t(nPaths) * dim * 8 + 8))) return rc;
+    CF_CUDA(cudaMemcpyAsync(d.ptr, dirs.data(), dirs.size() * 4, cudaMemcpyHostToDevice, ctx->c.stream));
+    rc = launch_gauss(useSobol, (const unsigned*)d.ptr, ctx->c.jumpA, ctx->c.jumpB, seed1, seed2, dim, firstPath,
+                      nPaths, (double*)o.ptr, ctx->c.stream);
+    if (rc) return cuda_fail(cudaError_t(rc), "gaussians");
+    CF_CUDA(cudaMemcpyAsync(out, o.ptr, size_t(nPaths) * dim * 8, cudaMemcpyDeviceToHost, ctx->c.stream));
+    CF_CUDA(cudaStreamSynchronize(ctx->c.stream));
+    d.release();
+    o.release();
+    return CF_OK;
+}
+
+}  // extern "C"

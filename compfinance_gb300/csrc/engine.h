@@ -1,0 +1,112 @@
+// Host engine types behind the C ABI: store entries, lowered plans, the context.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/cfgpu.h"
+#include "cf_params.h"
+
+namespace cf {
+
+int fail(int code, const std::string& msg);
+int cuda_fail(cudaError_t e, const char* what);
+double fix_value_host(long long hi, long long lo);
+
+struct DevBuf
+{
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    int ensure(size_t n);  // grows (never shrinks) the allocation
+    void release();
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { release(); }
+};
+
+// A model of the store (store.h:38-73): Black-Scholes or Dupire.
+struct ModelDesc
+{
+    int kind = MODEL_BS;
+    double spot = 0, vol = 0, rate = 0, div = 0;
+    bool qSpot = false;
+    std::vector<double> spots, times, vols;  // Dupire, vols spot-major
+    double maxDt = 0.25;
+    std::vector<std::string> labels;
+    unsigned long long version = 0;
+    void build();
+    int numParams() const;
+};
+
+// A product of the store (store.h:128-205): European, up-and-out, Europeans.
+struct ProductDesc
+{
+    int kind = PROD_EUROPEAN;
+    double strike = 0, exercise = 0, settlement = 0, barrier = 0, maturity = 0, freq = 0, smooth = 0;
+    int callPut = 0;
+    std::vector<double> mats, strikes;  // Europeans input pairs
+    // derived
+    std::vector<double> timeline, fwdMat, discMat, kflat;
+    std::vector<int> needNum, payOff;
+    std::vector<std::string> labels;
+    unsigned long long version = 0;
+    void build();
+};
+
+// The device tables of one (model, product) pair.
+struct Plan
+{
+    int model = 0, prod = 0, nSteps = 0, nEv = 0, nPay = 0, nParam = 0;
+    bool sobolOk = false;
+    size_t yBytesD = 0, yBytesF = 0;
+    unsigned long long mver = 0, pver = 0;
+    std::vector<double> timeline;
+    std::vector<int> evAtStep;
+    DevBuf tables;
+    McParams base;
+};
+
+struct Context
+{
+    int device = 0;
+    cudaStream_t ownStream = nullptr;
+    cudaStream_t stream = nullptr;
+    int numSMs = 0;
+    unsigned long long versionCounter = 0;
+    std::map<std::string, ModelDesc> models;
+    std::map<std::string, ProductDesc> products;
+    std::map<std::pair<std::string, std::string>, std::unique_ptr<Plan>> plans;
+    DevBuf jump, err, work, scratch;
+    const unsigned long long* jumpA = nullptr;
+    const unsigned long long* jumpB = nullptr;
+    std::vector<double> hostW;
+    // last enqueued run
+    McParams last;
+    McLaunch lastLaunch;
+    Plan* lastPlan = nullptr;
+    bool lastRisk = false;
+    int launches = 0;
+    unsigned long long h2d = 0, d2h = 0;  // cumulative transfer bytes
+
+    int init(int dev);
+    ~Context();
+    int getPlan(const std::string& mid, const std::string& pid, Plan*& out);
+    int buildPlan(const ModelDesc& m, const ProductDesc& pd, Plan& plan);
+    int enqueue(Plan& plan, const cf_num_param& num, bool risk, const double* weights);
+    int fetch(double* values, double* stderrs, double* aggregate, double* risks);
+    int riskMulti(Plan& plan, const cf_num_param& num, double* values, double* risks);
+};
+
+}  // namespace cf
+
+// The opaque handle of the C ABI.
+struct cf_context
+{
+    cf::Context c;
+    std::mutex mu;
+};

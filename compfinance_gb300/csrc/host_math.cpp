@@ -1,0 +1,174 @@
+// Host-side pieces of the reference's algorithms (see host_math.h).  Compiled with
+// -ffp-contract=off so the double arithmetic rounds exactly like the reference's.
+#include "host_math.h"
+
+#include <cstdio>
+#include <iterator>
+
+namespace cf {
+
+std::vector<double> fill_data(const std::vector<double>& original, double maxDx, double minDx,
+                              const std::vector<double>& add)
+{
+    std::vector<double> seq;
+    if (!add.empty())
+        std::set_union(original.begin(), original.end(), add.begin(), add.end(), std::back_inserter(seq),
+                       [minDx](double x, double y) { return x < y - minDx; });
+    else
+        seq = original;
+    std::vector<double> out;
+    if (seq.empty()) return out;
+    out.push_back(seq[0]);
+    for (size_t i = 1; i < seq.size(); ++i)
+    {
+        const double cur = out.back(), nxt = seq[i];
+        if (nxt - cur > maxDx)
+        {
+            const int n = int((nxt - cur) / maxDx - kEps) + 1;
+            const double h = (nxt - cur) / n;
+            for (double t = cur + h; t < nxt - minDx; t += h) out.push_back(t);
+        }
+        out.push_back(nxt);
+    }
+    return out;
+}
+
+double interp_lin(const double* x, size_t n, const double* y, double x0)
+{
+    const double* it = std::upper_bound(x, x + n, x0);
+    if (it == x + n) return y[n - 1];
+    if (it == x) return y[0];
+    const size_t k = size_t(it - x) - 1;
+    const double t = (x0 - x[k]) / (x[k + 1] - x[k]);
+    return y[k] + (y[k + 1] - y[k]) * t;
+}
+
+std::string fmt2(double x)
+{
+    char b[64];
+    std::snprintf(b, sizeof b, "%.2f", x);
+    return b;
+}
+
+namespace {
+struct JKInit
+{
+    int s, a;
+    unsigned m[13];
+};
+const JKInit kJK[] = {
+#include "../data/sobol_joe_kuo.inc"
+};
+}  // namespace
+
+int sobol_max_dim() { return CF_SOBOL_MAX_DIM; }
+
+std::vector<uint32_t> sobol_dirs(int dims)
+{
+    std::vector<uint32_t> d(size_t(32) * dims);
+    for (int dim = 0; dim < dims; ++dim)
+    {
+        const JKInit& e = kJK[dim];
+        uint64_t m[32];
+        if (e.s == 0)
+            for (int k = 0; k < 32; ++k) m[k] = 1;
+        else
+        {
+            for (int k = 0; k < e.s; ++k) m[k] = e.m[k];
+            for (int k = e.s; k < 32; ++k)
+            {
+                uint64_t v = m[k - e.s] ^ (m[k - e.s] << e.s);
+                for (int j = 1; j < e.s; ++j)
+                    if ((e.a >> (e.s - 1 - j)) & 1) v ^= m[k - j] << j;
+                m[k] = v;
+            }
+        }
+        for (int k = 0; k < 32; ++k) d[size_t(k) * dims + dim] = uint32_t(m[k] << (31 - k));
+    }
+    return d;
+}
+
+static void matmul_mod(const uint64_t a[9], const uint64_t b[9], uint64_t m, uint64_t r[9])
+{
+    uint64_t t[9];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+        {
+            unsigned __int128 s = 0;
+            for (int l = 0; l < 3; ++l) s += (unsigned __int128)a[3 * i + l] * b[3 * l + j];
+            t[3 * i + j] = uint64_t(s % m);
+        }
+    std::copy(t, t + 9, r);
+}
+
+void mrg_jump_tables(uint64_t A[64][9], uint64_t B[64][9])
+{
+    const uint64_t m1 = 4294967087ULL, m2 = 4294944443ULL;
+    uint64_t a[9] = {0, 1403580, m1 - 810728, 1, 0, 0, 0, 1, 0};
+    uint64_t b[9] = {527612, 0, m2 - 1370589, 1, 0, 0, 0, 1, 0};
+    for (int k = 0; k < 64; ++k)
+    {
+        std::copy(a, a + 9, A[k]);
+        std::copy(b, b + 9, B[k]);
+        matmul_mod(a, a, m1, a);
+        matmul_mod(b, b, m2, b);
+    }
+}
+
+double normal_dens(double x) { return x < -10.0 || 10.0 < x ? 0.0 : std::exp(-0.5 * x * x) / 2.506628274631; }
+
+double normal_cdf(double x)
+{
+    if (x < -10.0) return 0.0;
+    if (x > 10.0) return 1.0;
+    if (x < 0.0) return 1.0 - normal_cdf(-x);
+    const double t = 1.0 / (1.0 + 0.2316419 * x);
+    const double pol =
+        t * (0.319381530 + t * (-0.356563782 + t * (1.781477937 + t * (-1.821255978 + t * 1.330274429))));
+    return 1.0 - normal_dens(x) * pol;
+}
+
+double black_scholes(double spot, double strike, double vol, double mat)
+{
+    const double sd = vol * std::sqrt(mat);
+    if (sd <= kEps) return std::max(0.0, spot - strike);
+    const double d2 = std::log(spot / strike) / sd - 0.5 * sd;
+    const double d1 = d2 + sd;
+    return spot * normal_cdf(d1) - strike * normal_cdf(d2);
+}
+
+double black_scholes_ivol(double spot, double strike, double prem, double mat)
+{
+    if (prem <= std::max(0.0, spot - strike) + kEps) return 0.0;
+    double u = 0.5;
+    while (black_scholes(spot, strike, u, mat) < prem) u *= 2;
+    double l = 0.05;
+    while (black_scholes(spot, strike, l, mat) > prem) l /= 2;
+    double pu = black_scholes(spot, strike, u, mat), pl = black_scholes(spot, strike, l, mat);
+    while (u - l > 1.e-12)
+    {
+        const double m = 0.5 * (u + l), pm = black_scholes(spot, strike, m, mat);
+        if (pm > prem) { u = m; pu = pm; }
+        else { l = m; pl = pm; }
+    }
+    return l + (prem - pl) / (pu - pl) * (u - l);
+}
+
+double merton_price(double spot, double strike, double vol, double mat, double intens, double meanJmp,
+                    double stdJmp)
+{
+    const double varJmp = stdJmp * stdJmp, mv2 = meanJmp + 0.5 * varJmp, comp = intens * (std::exp(mv2) - 1),
+                 var = vol * vol, intensT = intens * mat;
+    unsigned fact = 1;
+    double iT = 1.0, res = 0.0;
+    for (size_t n = 0; n < 10; ++n)
+    {
+        const double s = spot * std::exp(n * mv2 - comp * mat), v = std::sqrt(var + n * varJmp / mat);
+        res += std::exp(-intensT) * iT / fact * black_scholes(s, strike, v, mat);
+        fact *= unsigned(n + 1);
+        iT *= intensT;
+    }
+    return res;
+}
+
+}  // namespace cf

@@ -1,0 +1,44 @@
+// Host-side pieces of the reference's algorithms that run once per model/product:
+// grid refinement, interpolation, timelines, Sobol direction numbers, mrg32k3a jump tables.
+#pragma once
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace cf {
+
+constexpr double kEps = 1.0e-08;                  // gaussians.h:8
+constexpr double kHalfDay = 0.00136986301369863;  // mcMdlDupire.h:26
+constexpr double kOneHour = 0.000114469;          // mcPrd.h:26
+
+// fillData, utility.h:11-79: the sorted union of `original` and `add` (points closer than
+// minDx merged), then extra points so that no gap exceeds maxDx.
+std::vector<double> fill_data(const std::vector<double>& original, double maxDx, double minDx,
+                              const std::vector<double>& add = {});
+
+// interp, interp.h:26-63 (linear or smoothstep, flat extrapolation) for double y.
+double interp_lin(const double* x, size_t n, const double* y, double x0);
+
+// "%.2f" as std::ostringstream << fixed << setprecision(2) prints it (mcPrd.h labels).
+std::string fmt2(double x);
+
+// Sobol direction numbers [32][dims] of the first `dims` dimensions, regenerated from the
+// Joe-Kuo initialisation data with the recurrence m_k = 2a_1 m_{k-1} ^ ... ^ 2^s m_{k-s} ^ m_{k-s}.
+int sobol_max_dim();
+std::vector<uint32_t> sobol_dirs(int dims);
+
+// A^(2^k) mod m1 and B^(2^k) mod m2 for k = 0..63 (row-major 3x3), the matrices of the
+// two mrg32k3a recurrences (mrg32k3a.h:319-358).
+void mrg_jump_tables(uint64_t A[64][9], uint64_t B[64][9]);
+
+// Black-Scholes formula, Zelen-Severo normal CDF, implied vol, Merton (analytics.h:8-91).
+double normal_cdf(double x);
+double normal_dens(double x);
+double black_scholes(double spot, double strike, double vol, double mat);
+double black_scholes_ivol(double spot, double strike, double prem, double mat);
+double merton_price(double spot, double strike, double vol, double mat, double intens, double meanJmp,
+                    double stdJmp);
+
+}  // namespace cf

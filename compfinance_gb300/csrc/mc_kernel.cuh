@@ -1,0 +1,581 @@
+// The Monte Carlo valuation / adjoint kernel.
+//
+// One thread owns a work unit: an antithetic pair of paths for mrg32k3a (both paths share
+// one Gaussian vector, the second negated: mrg32k3a.h:150-184), or one path for Sobol
+// (the 32 lanes of a warp take 32 consecutive Sobol indices).  Per unit the kernel runs
+//   forward:  Gaussians -> model step (Dupire log-Euler with linear interpolation in log
+//             spot, mcMdlDupire.h:238-280; or exact Black-Scholes steps, mcMdlBS.h:321-350)
+//             -> product events (mcPrd.h payoffs), storing the per-step state it needs later;
+//   reverse:  (risk launches) the hand-written adjoint of the same operations, step by step
+//             from maturity back to today, replacing the reference's tape
+//             (mcBase.h:427-532 records ~5 nodes per step and sweeps them back).
+// Node adjoints of the local-vol grid, parameter adjoints and payoff sums are added to a
+// block-private shared-memory slab in exact fixed point, flushed once per block.
+#pragma once
+#include <type_traits>
+
+#include "cf_device.cuh"
+
+namespace cf {
+
+constexpr int MC_BLOCK = 128;
+// FP32 risk runs flush their single-word node slab after this many units per thread
+// (<= 1024 paths per block between flushes), so no word can overflow.
+constexpr int NODE_FLUSH_UNITS = 4;
+
+template <class R>
+__device__ __forceinline__ const R* pick(const double* d, const float* f);
+template <>
+__device__ __forceinline__ const double* pick<double>(const double* d, const float*) { return d; }
+template <>
+__device__ __forceinline__ const float* pick<float>(const double*, const float* f) { return f; }
+
+__host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
+
+// Shared-memory carve-up; identical on host (sizing) and device (pointers).
+struct SmemLayout
+{
+    size_t slab, node, mbar, X, inv, bucket, Y, base, total;
+};
+
+__host__ __device__ inline SmemLayout mc_layout(int model, int rng, int fp32, int stageY, const McParams& p,
+                                                int block)
+{
+    SmemLayout L;
+    const size_t rs = fp32 ? 4 : 8;
+    size_t off = 0;
+    // slab: 4 scalar parameter adjoints + payoff / aggregate sums, two words each
+    L.slab = off;
+    off += align16(size_t(4 + 2 * p.nPay + 2) * 16);
+    // local-vol node adjoints: one word each in the FP32 form, two in the FP64 form
+    L.node = off;
+    if (model == MODEL_DUPIRE && p.nRisk > 0) off += align16(size_t(p.nS) * p.nT * (fp32 ? 8 : 16));
+    L.mbar = off;
+    off += 16;
+    L.X = L.inv = L.bucket = L.Y = L.base = off;
+    if (model == MODEL_DUPIRE)
+    {
+        L.X = off;
+        off += align16(size_t(p.nS) * rs);
+        L.inv = off;
+        off += align16(size_t(p.nS) * rs);
+        L.bucket = off;
+        off += align16(size_t(p.nBuckets) * 4);
+        L.Y = off;
+        if (stageY) off += align16(size_t(p.nSteps) * p.nS * rs);
+    }
+    L.base = off;
+    if (rng == RNG_SOBOL) off += align16(size_t(block / 32) * (size_t(p.nSteps) | 1) * 4);
+    L.total = off;
+    return L;
+}
+
+template <int MODEL, int PROD, int RNGK, class Real, bool RISK>
+__global__ void __launch_bounds__(MC_BLOCK) mc_kernel(const McParams p)
+{
+    constexpr int NP = RNGK == RNG_MRG ? 2 : 1;
+    constexpr bool F32 = std::is_same<Real, float>::value;
+    extern __shared__ __align__(128) unsigned char smem[];
+
+    const SmemLayout L = mc_layout(MODEL, RNGK, F32, p.stageY, p, MC_BLOCK);
+    long long* slab = reinterpret_cast<long long*>(smem + L.slab);  // scalar adjoints [0,4), payoffs from 8
+    long long* paySlab = slab + 8;
+    long long* node = reinterpret_cast<long long*>(smem + L.node);
+    const int tid = threadIdx.x;
+    const int nNodes = (MODEL == MODEL_DUPIRE && RISK) ? p.nS * p.nT : 0;
+    const int nodeWords = nNodes * (F32 ? 1 : 2);
+    for (int i = tid; i < 2 * (4 + 2 * p.nPay + 2); i += MC_BLOCK) slab[i] = 0;
+    for (int i = tid; i < nodeWords; i += MC_BLOCK) node[i] = 0;
+    int overflow = 0;
+
+    const int nSteps = p.nSteps;
+    const int nS = p.nS, nT = p.nT;
+    Real* sX = reinterpret_cast<Real*>(smem + L.X);
+    Real* sInv = reinterpret_cast<Real*>(smem + L.inv);
+    int* sBucket = reinterpret_cast<int*>(smem + L.bucket);
+    const Real* Y = pick<Real>(p.Yd, p.Yf);
+    if (MODEL == MODEL_DUPIRE)
+    {
+        const Real* gX = pick<Real>(p.Xd, p.Xf);
+        const Real* gI = pick<Real>(p.invdXd, p.invdXf);
+        for (int i = tid; i < nS; i += MC_BLOCK)
+        {
+            sX[i] = gX[i];
+            sInv[i] = gI[i];
+        }
+        for (int i = tid; i < p.nBuckets; i += MC_BLOCK) sBucket[i] = p.bucket[i];
+        if (p.stageY)
+        {
+            Real* sY = reinterpret_cast<Real*>(smem + L.Y);
+            const unsigned bytes = (unsigned)align16(size_t(nSteps) * nS * sizeof(Real));
+            if (bulk_copy_to_smem(sY, Y, bytes, reinterpret_cast<unsigned long long*>(smem + L.mbar), p.err))
+                Y = sY;
+        }
+    }
+    __syncthreads();
+
+    const Real* bs = pick<Real>(p.bsD, p.bsF);
+    const Real* ev = pick<Real>(p.evD, p.evF);
+    const Real* kK = pick<Real>(p.kD, p.kF);
+    const Real* cA = pick<Real>(p.cAd, p.cAf);
+    const Real* cB = pick<Real>(p.cBd, p.cBf);
+    const Real* wts = pick<Real>(p.w, p.wf);
+    const int nEv = p.nEv;
+    const int nPay = p.nPay;
+    const int payBase = 0, sqBase = nPay, aggBase = 2 * nPay;  // in paySlab
+    const Real strike = (Real)p.strike, barSmooth = (Real)p.barSmooth, minusSmooth = (Real)p.minusSmooth,
+               twoSmooth = (Real)p.twoSmooth;
+    const Real logBand = F32 ? (Real)p.logBandF : (Real)p.logBandD;
+    // state variable: FP64 form x = log S; FP32 form y = log S - log spot, S = s0 * exp(y)
+    const Real xStart = F32 ? Real(0) : (Real)p.x0d;
+    const Real sScale = F32 ? (Real)p.s0f : Real(1);
+    const Real spot = (Real)p.spot;
+    const Real w0 = nPay > 0 ? wts[0] : Real(0), w1 = nPay > 1 ? wts[1] : Real(0);
+
+    const long long T = (long long)gridDim.x * MC_BLOCK;
+    const long long tg = (long long)blockIdx.x * MC_BLOCK + tid;
+    // scratch element (field f, timeline point i) of this thread; the host keeps the whole
+    // scratch below 2^31 elements so the offsets are 32-bit
+    Real* scr = reinterpret_cast<Real*>(p.scratch) + tg;
+    const int Ti = int(T);
+    const int rowStride = (nSteps + 1) * Ti;
+    auto SCR = [&](int f, int i) -> Real& { return scr[f * rowStride + i * Ti]; };
+    constexpr int F_G = 0, F_X = 1, F_AL = 1 + NP;
+
+    auto spotOf = [&](Real xs) -> Real {
+        if (MODEL == MODEL_DUPIRE) return sScale * exp(xs);
+        return xs;
+    };
+
+    // Interpolation of row s of Y at state xs: first knot above xs (upper_bound), linear
+    // weight t, value v and slope dv/dx; flat extrapolation at both ends (interp.h:26-63).
+    const Real bX0 = F32 ? (Real)p.bX0f : (Real)p.bX0d;
+    const Real bInvW = F32 ? (Real)p.bInvWf : (Real)p.bInvWd;
+    const int nB = p.nBuckets;
+    auto interpRow = [&](int s, Real xs, int& k, Real& t, Real& v, Real& slope, bool& flat) {
+        // upper_bound(X, xs): bucket guess, then exact adjustment in both directions
+        const Real fb = (xs - bX0) * bInvW;
+        int b = fb > Real(0) ? int(fb) : 0;
+        b = b < nB - 1 ? b : nB - 1;
+        int lo = sBucket[b];
+        while (lo < nS && !(sX[lo] > xs)) ++lo;
+        while (lo > 0 && sX[lo - 1] > xs) --lo;
+        const Real* row = Y + size_t(s) * nS;
+        if (lo == nS || lo == 0)
+        {
+            k = lo == 0 ? 0 : nS - 1;
+            flat = true;
+            t = Real(0);
+            v = row[k];
+            slope = Real(0);
+        }
+        else
+        {
+            k = lo - 1;
+            flat = false;
+            const Real y1 = row[k], y2 = row[k + 1];
+            t = (xs - sX[k]) * sInv[k];
+            v = y1 + (y2 - y1) * t;
+            slope = (y2 - y1) * sInv[k];
+        }
+    };
+
+    // ---------------------------------------------------------------------------------
+    // One work unit: nAct (1 or 2) paths driven by the Gaussian generator gen(i).
+    // ---------------------------------------------------------------------------------
+    auto runUnit = [&](int nAct, auto&& gen) {
+        Real x[NP], alive[NP], euro[NP], fE[NP], dE[NP], nE[NP], agg[NP];
+        bool dead[NP];
+#pragma unroll
+        for (int a = 0; a < NP; ++a)
+        {
+            x[a] = MODEL == MODEL_DUPIRE ? xStart : spot;
+            alive[a] = Real(1);
+            euro[a] = fE[a] = dE[a] = Real(0);
+            nE[a] = Real(1);
+            agg[a] = Real(0);
+            dead[a] = false;
+        }
+
+        // forward event handling at timeline point i for product date e
+        auto eventFwd = [&](int e, int i, int a) {
+            const bool last = e == nEv - 1;
+            Real S;
+            // Up-and-out on Dupire: below the smoothing band (tested in log space with a margin
+            // that dominates exp/log rounding) a monitoring date changes nothing.
+            if (PROD == PROD_UOC && MODEL == MODEL_DUPIRE && !last && (dead[a] || !(x[a] > logBand))) return;
+            S = spotOf(x[a]);
+            Real F = S, D = Real(1), N = Real(1);
+            if (MODEL == MODEL_BS)
+            {
+                F = S * ev[e];
+                D = ev[2 * nEv + e];
+                if (ev[6 * nEv + e] != Real(0)) N = p.spotMeasure ? ev[4 * nEv + e] * S : ev[4 * nEv + e];
+            }
+            if (PROD == PROD_EUROPEAN)
+            {
+                fE[a] = F;
+                dE[a] = D;
+                nE[a] = N;
+            }
+            else if (PROD == PROD_UOC)
+            {
+                if (!dead[a])
+                {
+                    if (F > barSmooth) dead[a] = true;
+                    else if (F > minusSmooth)
+                    {
+                        if (RISK) SCR(F_AL + a, i) = alive[a];
+                        alive[a] *= (barSmooth - F) / twoSmooth;
+                    }
+                }
+                if (last)
+                {
+                    fE[a] = F;
+                    nE[a] = N;
+                    const Real m = p.callPut ? (strike - F) : (F - strike);
+                    euro[a] = (m > Real(0) ? m : Real(0)) / N;
+                }
+            }
+            else
+            {
+                const int k0 = p.evPayOff[e], k1 = p.evPayOff[e + 1];
+                for (int k = k0; k < k1; ++k)
+                {
+                    const Real m = F - kK[k];
+                    const Real pay = (m > Real(0) ? m : Real(0)) / N;
+                    if (pay != Real(0))
+                    {
+                        fix_add(&paySlab[2 * (payBase + k)], pay);
+                        fix_add(&paySlab[2 * (sqBase + k)], pay * pay);
+                    }
+                    if (RISK) agg[a] += wts[k] * pay;
+                }
+            }
+        };
+
+        {
+            const int e0 = p.evAtStep[0];
+            if (e0 >= 0)
+                #pragma unroll
+                for (int a = 0; a < NP; ++a)
+                    if (a < nAct) eventFwd(e0, 0, a);
+        }
+        for (int i = 0; i < nSteps; ++i)
+        {
+            const Real g = gen(i);
+            if (RISK) SCR(F_G, i) = g;
+#pragma unroll
+            for (int a = 0; a < NP; ++a)
+            {
+                if (a >= nAct) break;
+                const Real ga = a ? -g : g;
+                if (RISK) SCR(F_X + a, i) = x[a];
+                if (MODEL == MODEL_DUPIRE)
+                {
+                    int k;
+                    Real t, v, slope;
+                    bool flat;
+                    interpRow(i, x[a], k, t, v, slope, flat);
+                    x[a] += v * (Real(-0.5) * v + ga);
+                }
+                else
+                {
+                    x[a] = x[a] * exp(bs[i] + bs[nSteps + i] * ga);
+                }
+            }
+            const int e = p.evAtStep[i + 1];
+            if (e >= 0)
+                #pragma unroll
+                for (int a = 0; a < NP; ++a)
+                    if (a < nAct) eventFwd(e, i + 1, a);
+        }
+
+        // payoffs and value sums
+#pragma unroll
+        for (int a = 0; a < NP; ++a)
+        {
+            if (a >= nAct) break;
+            if (PROD == PROD_EUROPEAN)
+            {
+                const Real m = fE[a] - strike;
+                const Real pay = (m > Real(0) ? m : Real(0)) * dE[a] / nE[a];
+                fix_add(&paySlab[2 * payBase], pay);
+                fix_add(&paySlab[2 * sqBase], pay * pay);
+                agg[a] = w0 * pay;
+            }
+            else if (PROD == PROD_UOC)
+            {
+                const Real p0 = dead[a] ? Real(0) : alive[a] * euro[a];
+                fix_add(&paySlab[2 * payBase], p0);
+                fix_add(&paySlab[2 * sqBase], p0 * p0);
+                fix_add(&paySlab[2 * (payBase + 1)], euro[a]);
+                fix_add(&paySlab[2 * (sqBase + 1)], euro[a] * euro[a]);
+                agg[a] = w0 * p0 + w1 * euro[a];
+            }
+            if (RISK)
+            {
+                fix_add(&paySlab[2 * aggBase], agg[a]);
+                fix_add(&paySlab[2 * (aggBase + 1)], agg[a] * agg[a]);
+            }
+        }
+        if (!RISK) return;
+
+        // ---------------------------------------------------------------------------
+        // Reverse sweep.
+        // ---------------------------------------------------------------------------
+        Real ax[NP], aAlive[NP], aEuro[NP], aVol[NP], aR[NP], aDv[NP], aSp[NP];
+#pragma unroll
+        for (int a = 0; a < NP; ++a)
+        {
+            ax[a] = aVol[a] = aR[a] = aDv[a] = aSp[a] = Real(0);
+            aEuro[a] = dead[a] ? w1 : w0 * alive[a] + w1;       // payoff0 = alive*euro, payoff1 = euro
+            aAlive[a] = dead[a] ? Real(0) : w0 * euro[a];
+        }
+        for (int i = nSteps; i >= 0; --i)
+        {
+            const int e = p.evAtStep[i];
+            if (e >= 0)
+            {
+#pragma unroll
+                for (int a = 0; a < NP; ++a)
+                {
+                    if (a >= nAct) break;
+                    const Real xi = i == nSteps ? x[a] : SCR(F_X + a, i);
+                    const bool last = e == nEv - 1;
+                    if (PROD == PROD_UOC && MODEL == MODEL_DUPIRE && !last && (dead[a] || !(xi > logBand)))
+                        continue;
+                    const Real S = spotOf(xi);
+                    Real F = S, D = Real(1), N = Real(1), ff = Real(1), nf = Real(0);
+                    const bool needN = MODEL == MODEL_BS ? ev[6 * nEv + e] != Real(0) : false;
+                    if (MODEL == MODEL_BS)
+                    {
+                        ff = ev[e];
+                        F = S * ff;
+                        D = ev[2 * nEv + e];
+                        nf = ev[4 * nEv + e];
+                        if (needN) N = p.spotMeasure ? nf * S : nf;
+                    }
+                    Real aF = Real(0), aD = Real(0), aN = Real(0);
+                    if (PROD == PROD_EUROPEAN)
+                    {
+                        const Real m = F - strike;
+                        if (m > Real(0))
+                        {
+                            aF = w0 * D / N;
+                            aD = w0 * m / N;
+                            aN = -w0 * m * D / (N * N);
+                        }
+                    }
+                    else if (PROD == PROD_UOC)
+                    {
+                        if (last)
+                        {
+                            const Real m = p.callPut ? (strike - F) : (F - strike);
+                            if (m > Real(0))
+                            {
+                                aF = (p.callPut ? -aEuro[a] : aEuro[a]) / N;
+                                aN = -aEuro[a] * m / (N * N);
+                            }
+                        }
+                        if (!dead[a] && F > minusSmooth)
+                        {
+                            const Real before = SCR(F_AL + a, i);
+                            aF += aAlive[a] * before * (Real(-1) / twoSmooth);
+                            aAlive[a] *= (barSmooth - F) / twoSmooth;
+                        }
+                    }
+                    else
+                    {
+                        const int k0 = p.evPayOff[e], k1 = p.evPayOff[e + 1];
+                        for (int k = k0; k < k1; ++k)
+                        {
+                            const Real m = F - kK[k];
+                            if (m > Real(0))
+                            {
+                                aF += wts[k] / N;
+                                aN -= wts[k] * m / (N * N);
+                            }
+                        }
+                    }
+                    if (MODEL == MODEL_DUPIRE)
+                    {
+                        ax[a] += aF * S;  // F = S = exp(x)
+                    }
+                    else
+                    {
+                        const Real tauF = ev[nEv + e], tauD = ev[3 * nEv + e], te = ev[5 * nEv + e];
+                        ax[a] += aF * ff;
+                        const Real aff = aF * S * ff;  // d ff / d mu = tauF * ff
+                        aR[a] += aff * tauF;
+                        aDv[a] -= aff * tauF;
+                        aR[a] -= aD * D * tauD;       // D = exp(-r tauD)
+                        if (needN)
+                        {
+                            if (p.spotMeasure)        // N = exp(d t) / spot * S
+                            {
+                                ax[a] += aN * nf;
+                                aDv[a] += aN * N * te;
+                                aSp[a] -= aN * N / spot;
+                            }
+                            else                      // N = exp(r t)
+                                aR[a] += aN * N * te;
+                        }
+                    }
+                }
+            }
+            if (i == 0) break;
+            const int s = i - 1;
+            const Real g = SCR(F_G, s);
+#pragma unroll
+            for (int a = 0; a < NP; ++a)
+            {
+                if (a >= nAct) break;
+                const Real ga = a ? -g : g;
+                const Real xs = SCR(F_X + a, s);
+                if (MODEL == MODEL_DUPIRE)
+                {
+                    int k;
+                    Real t, v, slope;
+                    bool flat;
+                    interpRow(s, xs, k, t, v, slope, flat);
+                    const Real q = ga - v;             // d x_{s+1} / d v
+                    const Real av = ax[a] * q;
+                    ax[a] += av * slope;               // d x_{s+1} / d x_s = 1 + q dv/dx
+                    const int ca = p.colA[s], cb = p.colB[s];
+                    const Real wa = cA[s], wb = cB[s];
+                    auto put = [&](int j, Real aY) {
+                        if (aY == Real(0)) return;
+                        if (F32)
+                        {
+                            fix1_add(&node[j * nT + ca], float(aY * wa), &p.acc[2 * (1 + j * nT + ca)]);
+                            if (wb != Real(0))
+                                fix1_add(&node[j * nT + cb], float(aY * wb), &p.acc[2 * (1 + j * nT + cb)]);
+                        }
+                        else
+                        {
+                            fix_add(&node[2 * (j * nT + ca)], aY * wa);
+                            if (wb != Real(0)) fix_add(&node[2 * (j * nT + cb)], aY * wb);
+                        }
+                    };
+                    if (flat) put(k, av);
+                    else
+                    {
+                        put(k, av * (Real(1) - t));
+                        put(k + 1, av * t);
+                    }
+                }
+                else
+                {
+                    const Real E = exp(bs[s] + bs[nSteps + s] * ga);
+                    const Real aArg = ax[a] * (xs * E);  // d S_{s+1} / d(drift + std g) = S_{s+1}
+                    aVol[a] += aArg * bs[4 * nSteps + s] + aArg * ga * bs[3 * nSteps + s];
+                    aR[a] += aArg * bs[2 * nSteps + s];
+                    aDv[a] -= aArg * bs[2 * nSteps + s];
+                    ax[a] *= E;
+                }
+            }
+        }
+        if (MODEL == MODEL_DUPIRE)
+        {
+            Real sp = Real(0);
+#pragma unroll
+            for (int a = 0; a < NP; ++a)
+                if (a < nAct) sp += ax[a];
+            fix_add(&slab[0], sp / spot);  // x_0 = log(spot)
+        }
+        else
+        {
+            Real s0 = 0, s1 = 0, s2 = 0, s3 = 0;
+#pragma unroll
+            for (int a = 0; a < NP; ++a)
+            {
+                if (a >= nAct) break;
+                s0 += ax[a] + aSp[a];
+                s1 += aVol[a];
+                s2 += aR[a];
+                s3 += aDv[a];
+            }
+            fix_add(&slab[0], s0);
+            fix_add(&slab[2], s1);
+            fix_add(&slab[4], s2);
+            fix_add(&slab[6], s3);
+        }
+    };
+
+    // Single-word node words flushed to the global hi/lo accumulators (block-wide).
+    auto flushNodes = [&]() {
+        __syncthreads();
+        for (int i = tid; i < nNodes; i += MC_BLOCK)
+        {
+            fix1_flush(&p.acc[2 * (1 + i)], node[i]);
+            node[i] = 0;
+        }
+        __syncthreads();
+    };
+
+    if (RNGK == RNG_MRG)
+    {
+        const long long nUnits = (p.nPath + 1) / 2;
+        const long long per = (nUnits + T - 1) / T;
+        const long long u0 = tg * per;
+        const long long u1 = u0 + per < nUnits ? u0 + per : nUnits;
+        MrgState st{};
+        if (u0 < u1) st = mrg_jump(p.seed1, p.seed2, (unsigned long long)u0 * nSteps, p.mrgJumpA, p.mrgJumpB);
+        // uniform trip count across the block so that the node slab can be flushed in step
+        for (long long it = 0; it < per; ++it)
+        {
+            const long long u = u0 + it;
+            if (u < u1)
+            {
+                const int nAct = (2 * u + 1 < p.nPath) ? 2 : 1;
+                runUnit(nAct, [&](int) { return mrg_gauss<Real>(mrg_next(st)); });
+            }
+            if (F32 && nNodes && (it + 1) % NODE_FLUSH_UNITS == 0) flushNodes();
+        }
+    }
+    else
+    {
+        // Sobol: warp w of the grid takes batches b = w, w + W, ...; lane l runs index
+        // n = 32b + l (path n-1).  state(n) = state(32b) ^ state(l) (gray code is linear
+        // over the disjoint bit ranges of 32b and l).
+        const int lane = tid & 31, wib = tid >> 5;
+        const int pitch = nSteps | 1;
+        unsigned* base = reinterpret_cast<unsigned*>(smem + L.base) + wib * pitch;
+        const long long W = T / 32, gw = tg / 32;
+        const long long nBatches = p.nPath / 32 + 1;
+        const long long rounds = (nBatches + W - 1) / W;
+        for (long long it = 0; it < rounds; ++it)
+        {
+            const long long b = gw + it * W;
+            if (F32 && nNodes && it > 0 && it % NODE_FLUSH_UNITS == 0) flushNodes();
+            if (b >= nBatches) continue;
+            __syncwarp();
+            for (int d = lane; d < nSteps; d += 32)
+                base[d] = sobol_state(p.sobolDir, nSteps, d, (unsigned long long)b * 32);
+            __syncwarp();
+            const long long n = b * 32 + lane;
+            if (n >= 1 && n <= p.nPath)
+                runUnit(1, [&](int i) {
+                    return sobol_gauss<Real>(base[i] ^ sobol_state(p.sobolDir, nSteps, i, (unsigned long long)lane));
+                });
+        }
+    }
+
+    __syncthreads();
+    // flush: scalar parameter adjoints, node adjoints, payoff sums
+    if (RISK)
+    {
+        const int nScal = MODEL == MODEL_BS ? 4 : 1;
+        for (int i = tid; i < nScal; i += MC_BLOCK) fix_flush(&p.acc[2 * i], &slab[2 * i]);
+        for (int i = tid; i < nNodes; i += MC_BLOCK)
+        {
+            if (F32) fix1_flush(&p.acc[2 * (1 + i)], node[i]);
+            else fix_flush(&p.acc[2 * (1 + i)], &node[2 * i]);
+        }
+    }
+    for (int i = tid; i < 2 * nPay + 2; i += MC_BLOCK) fix_flush(&p.acc[2 * (p.nRisk + i)], &paySlab[2 * i]);
+    if (overflow) atomicOr(p.err, DEVERR_FIXED_RANGE);
+}
+
+}  // namespace cf

@@ -1,0 +1,161 @@
+/* cfgpu.h -- C ABI of the GB300 Monte Carlo valuation and AAD-risk engine.
+ *
+ * Drop-in boundary for CompFinance's simulation path (main.h / store.h / mcBase.h):
+ * plain C types, caller-allocated outputs, an int status on every call, no exceptions.
+ * Every entry point names the reference interface it replaces.  The C++17 wrapper in
+ * cfgpu.hpp rebuilds the reference's own signatures (value, AADriskOne, AADriskMulti,
+ * dupireSuperbucket, put*) on top of these.
+ *
+ * Threading: one context per process is the normal use; calls on one context are
+ * serialised by an internal lock.  All device memory is owned by the context.
+ */
+#ifndef CFGPU_H
+#define CFGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------------------- */
+#define CF_OK 0
+#define CF_E_ARG (-1)        /* invalid argument (null pointer, bad size) */
+#define CF_E_NOTFOUND (-2)   /* unknown model / product id or payoff label */
+#define CF_E_SHAPE (-3)      /* output buffer too small / incompatible model and product */
+#define CF_E_CUDA (-4)       /* CUDA runtime error (message in cf_last_error) */
+#define CF_E_NOMEM (-5)      /* device allocation failed */
+#define CF_E_DEVICE (-6)     /* a kernel reported an error flag (bounded wait expired, range) */
+#define CF_E_UNSUPPORTED (-7)
+
+/* Precision of the path arithmetic: CF_FP64 is the parity form (matches the reference to
+ * ~1e-12); CF_FP32 keeps the path in FP32 and every sum in exact fixed point. */
+#define CF_FP64 0
+#define CF_FP32 1
+
+/* NumericalParam, main.h:33-40 (parallel is accepted and ignored: the GPU is always
+ * parallel), plus the precision of the path arithmetic. */
+typedef struct {
+    int parallel;
+    int useSobol;
+    int numPath;
+    int seed1;     /* default 12345 */
+    int seed2;     /* default 1234  */
+    int precision; /* CF_FP64 or CF_FP32 */
+} cf_num_param;
+
+typedef struct cf_context cf_context;
+
+/* ---- context --------------------------------------------------------------------- */
+/* Creates a context on CUDA device `device` (replaces the process-wide store and thread
+ * pool of store.h:33-36 / threadPool.h:72). */
+int cf_create(int device, cf_context** ctx);
+int cf_destroy(cf_context* ctx);
+/* Copies the last error message of this thread into buf (always NUL-terminated). */
+int cf_last_error(char* buf, size_t size);
+/* Sets the CUDA stream (cudaStream_t) of subsequent launches; NULL = the context's own. */
+int cf_set_stream(cf_context* ctx, void* stream);
+int cf_synchronize(cf_context* ctx);
+/* Cumulative bytes this context copied host->device and device->host (model tables,
+ * weights, results); for end-to-end accounting. */
+int cf_transfer_stats(cf_context* ctx, uint64_t* h2dBytes, uint64_t* d2hBytes);
+
+/* ---- store (store.h) -------------------------------------------------------------- */
+/* putBlackScholes, store.h:38-54 */
+int cf_put_black_scholes(cf_context* ctx, double spot, double vol, int qSpot, double rate, double div,
+                         const char* id);
+/* putDupire, store.h:56-73; vols spot-major [nSpots][nTimes] */
+int cf_put_dupire(cf_context* ctx, double spot, const double* spots, int nSpots, const double* times,
+                  int nTimes, const double* vols, double maxDt, const char* id);
+/* putEuropean, store.h:128-142 */
+int cf_put_european(cf_context* ctx, double strike, double exerciseDate, double settlementDate,
+                    const char* id);
+/* putBarrier, store.h:144-163 (smooth <= 0 is replaced by 1e-8 as in the reference) */
+int cf_put_barrier(cf_context* ctx, double strike, double barrier, double maturity, double monitorFreq,
+                   double smooth, int callPut, const char* id);
+/* putEuropeans, store.h:184-205 (maturities in increasing order) */
+int cf_put_europeans(cf_context* ctx, const double* maturities, const double* strikes, int n,
+                     const char* id);
+
+/* Product::payoffLabels (mcBase.h:137) and Model::parameterLabels (mcBase.h:194): labels
+ * written '\n'-separated into buf (NUL-terminated); *count receives their number.  With
+ * buf == NULL, *needed receives the buffer size. */
+int cf_payoff_labels(cf_context* ctx, const char* productId, char* buf, size_t size, int* count,
+                     size_t* needed);
+int cf_parameter_labels(cf_context* ctx, const char* modelId, char* buf, size_t size, int* count,
+                        size_t* needed);
+/* Sizes: number of payoffs, of model parameters, Gaussians per path (Model::simDim). */
+int cf_shapes(cf_context* ctx, const char* modelId, const char* productId, int* nPay, int* nParam,
+              int* simDim);
+
+/* ---- entry points (main.h) --------------------------------------------------------- */
+/* value, main.h:43-96: path averages of every payoff; stderrs (optional) are the Monte
+ * Carlo standard errors. */
+int cf_value(cf_context* ctx, const char* modelId, const char* productId, const cf_num_param* num,
+             double* values, double* stderrs);
+
+/* AADriskOne, main.h:99-173: risks[nParam] of the payoff labelled riskPayoff (NULL or ""
+ * = first payoff); payoffValues[nPay]; *riskPayoffValue its value. */
+int cf_aad_risk_one(cf_context* ctx, const char* modelId, const char* productId, const cf_num_param* num,
+                    const char* riskPayoff, double* payoffValues, double* riskPayoffValue, double* risks);
+
+/* AADriskAggregate, main.h:176-254: risks of sum_k notionals[k] * payoff_k; notionals[nPay]
+ * indexed like the payoff labels. */
+int cf_aad_risk_aggregate(cf_context* ctx, const char* modelId, const char* productId,
+                          const double* notionals, const cf_num_param* num, double* payoffValues,
+                          double* aggregateValue, double* risks);
+
+/* AADriskMulti, main.h:269-312: values[nPay], risks[nParam * nPay] parameter-major. */
+int cf_aad_risk_multi(cf_context* ctx, const char* modelId, const char* productId, const cf_num_param* num,
+                      double* values, double* risks);
+
+/* Implied-vol surfaces for the Dupire calibration (ivs.h): kind 0 =
+ * iv(K,T) = p0 + p1 ln^2(K/p3)/sqrt(T) + p2 ln(K/p3); kind 1 = MertonIVS (ivs.h:147-179)
+ * with p = {vol, jump intensity, mean jump, jump std}. */
+typedef struct {
+    int kind;
+    double spot;
+    double p[4];
+} cf_ivs;
+
+/* dupireCalib, mcMdlDupire.h:337-388 / main.h:414-438.  First call with lvols == NULL to
+ * get the grid sizes; lvols spot-major [nS][nT]. */
+int cf_dupire_calib(cf_context* ctx, const cf_ivs* ivs, const double* inclSpots, int nInclSpots,
+                    double maxDs, const double* inclTimes, int nInclTimes, double maxDtVol, int* nS, int* nT,
+                    double* spots, double* times, double* lvols);
+
+/* dupireSuperbucket, main.h:453-569: calibrate, Monte Carlo adjoints to the local vols
+ * (microbucket), then the adjoint of the calibration to the risk view's implied-vol
+ * spreads.  vega[nStrikes * nMats]; microbucket[nS * nT] optional.  refSeeding = 1
+ * reproduces the reference's seeding of the calibration tape by assignment (main.h:541-547),
+ * under which flat-extrapolated local vols overwrite instead of add; 0 is the exact adjoint. */
+int cf_dupire_superbucket(cf_context* ctx, const cf_ivs* ivs, double spot, double maxDt, const char* productId,
+                          const double* notionals, const double* inclSpots, int nInclSpots, double maxDs,
+                          const double* inclTimes, int nInclTimes, double maxDtVol, const double* strikes,
+                          int nStrikes, const double* mats, int nMats, const cf_num_param* num, int refSeeding,
+                          double* value, double* delta, double* vega, double* microbucket);
+
+/* ---- RNG access (sobol.h, mrg32k3a.h), for bit-exactness checks -------------------- */
+/* Sobol integer points of paths [firstPath, firstPath+nPaths), dimension dim: out[nPaths*dim]. */
+int cf_sobol_points(cf_context* ctx, int dim, int64_t firstPath, int nPaths, uint32_t* out);
+/* mrg32k3a state (x0,x1,x2,y0,y1,y2) before path firstPath (even) for dimension dim. */
+int cf_mrg_state(cf_context* ctx, unsigned seed1, unsigned seed2, int dim, int64_t firstPath, uint32_t* state6);
+/* Gaussians of paths [firstPath, firstPath+nPaths): out[nPaths*dim] (FP64 form). */
+int cf_gaussians(cf_context* ctx, int useSobol, unsigned seed1, unsigned seed2, int dim, int64_t firstPath,
+                 int nPaths, double* out);
+
+/* ---- device-resident launches (benchmarks and the serving loop) --------------------- */
+/* Enqueues the risk (risk=1, weights[nPay]) or value (risk=0) kernel of (model, product)
+ * on the context's stream without synchronising; results stay on the device until
+ * cf_fetch_result.  Returns the number of kernel launches enqueued in *launches. */
+int cf_enqueue(cf_context* ctx, const char* modelId, const char* productId, const cf_num_param* num, int risk,
+               const double* weights, int* launches);
+/* Synchronises and converts the last enqueued run: values[nPay], stderrs[nPay] (optional),
+ * aggregate (optional), risks[nParam] (risk runs, optional). */
+int cf_fetch_result(cf_context* ctx, double* values, double* stderrs, double* aggregate, double* risks);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CFGPU_H */

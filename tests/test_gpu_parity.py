@@ -1,0 +1,168 @@
+"""Parity of the CUDA engine (through the C ABI) with the reference.
+
+* RNG: Sobol integer points and mrg32k3a states bit-exact; Gaussians within 1 ulp-level.
+* FP64 form: prices and risks of every golden case within 1e-12 (relative to the largest
+  entry) of the reference's own mcSimul / mcSimulAAD results on the same RNG sequence.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from compfinance_gb300 import Engine
+from gpu_util import num, put_model, put_product, rel_to_max
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-12
+
+
+@pytest.fixture(scope="module")
+def eng():
+    e = Engine(0)
+    yield e
+    e.close()
+
+
+def test_sobol_points_bit_exact(eng, golden):
+    g = golden("rng")
+    assert (eng.sobolPoints(1101, 0, 3) == np.array(g["sobol_1101"], dtype=np.uint32)).all()
+    assert (eng.sobolPoints(8, 0, 300) == np.array(g["sobol_8"], dtype=np.uint32)).all()
+    for c in g["sobol_skip"]:
+        assert (eng.sobolPoints(c["dim"], c["b"], 1)[0] == np.array(c["ints"], dtype=np.uint32)).all(), c["b"]
+    # large indices against the oracle (skip-ahead by gray code)
+    for first in (123456789, (1 << 30) + 12345):
+        assert (eng.sobolPoints(64, first, 40) == O.sobol_ints(64, first, 40)).all()
+
+
+def test_mrg_states_bit_exact(eng, golden):
+    for c in golden("rng")["mrg_skip"]:
+        st = eng.mrgState(c["seed1"], c["seed2"], c["dim"], c["b"])
+        assert list(st) == c["state"], c["b"]
+    for first in (0, 2, 1 << 21, (1 << 40) + 6):
+        assert list(eng.mrgState(12345, 1234, 156, first)) == list(O.mrg_state(12345, 1234, 156, first))
+
+
+def test_gaussians(eng, golden):
+    seq = [s for s in golden("rng")["mrg_seq"] if s["kind"] == "g"][0]
+    got = eng.gaussians(False, seq["seed1"], seq["seed2"], seq["dim"], 0, len(seq["seq"]))
+    ref = np.array([r["v"] for r in seq["seq"]])
+    # The uniforms are bit-exact; the inverse normal differs from glibc's by a few ulps
+    # (CUDA's double log, and FMA contraction of the Beasley-Springer-Moro polynomials).
+    assert (np.abs(got - ref) <= 16 * np.spacing(np.abs(ref))).all()
+    for sob in (0, 1):
+        got = eng.gaussians(sob, 12345, 1234, 36, 1000, 200)
+        ref = O.sobol_gauss(36, 1000, 200) if sob else O.mrg_gauss(12345, 1234, 36, 1000, 200)
+        assert (np.abs(got - ref) <= 16 * np.spacing(np.abs(ref))).all()
+        assert (got == ref).mean() > 0.5
+
+
+@pytest.fixture(scope="module")
+def mc_eng(eng, golden):
+    d = golden("mc")
+    for mid, spec in d["models"].items():
+        put_model(eng, mid, spec)
+    for pid, spec in d["products"].items():
+        put_product(eng, pid, spec)
+    return eng, d
+
+
+def test_labels(mc_eng, golden):
+    eng, _ = mc_eng
+    for t in golden("host")["timelines"]:
+        assert eng.payoffLabels(t["product"]) == t["payoff_labels"]
+        assert eng.parameterLabels(t["model"]) == t["param_labels"]
+        _, _, dim = eng.shapes(t["model"], t["product"])
+        assert dim == len(t["sim_timeline"]) - 1
+
+
+def _weights(c, npay):
+    w = np.zeros(npay)
+    if c["mode"] == "risk":
+        w[c["payoff"]] = 1.0
+    else:
+        for k, x in c["notionals"]:
+            w[k] = x
+    return w
+
+
+def test_fp64_parity_with_reference(mc_eng):
+    eng, d = mc_eng
+    worst = {}
+    for c in d["cases"]:
+        nm = num(c["sobol"], c["npath"])
+        mid, pid = c["model"], c["product"]
+        npay, npar, _ = eng.shapes(mid, pid)
+        if c["mode"] == "value":
+            r = eng.value(mid, pid, nm)
+            err = rel_to_max(r["values"], c["values"])
+        elif c["mode"] in ("risk", "agg"):
+            labels = eng.payoffLabels(pid)
+            if c["mode"] == "risk":
+                r = eng.AADriskOne(mid, pid, nm, labels[c["payoff"]])
+            else:
+                r = eng.AADriskAggregate(mid, pid, _weights(c, npay), nm)
+            err = max(rel_to_max(r["payoffValues"], c["values"]),
+                      abs(r["riskPayoffValue"] - c["risk_value"]) / abs(c["risk_value"]),
+                      rel_to_max(r["risks"], c["risks"]))
+        else:
+            r = eng.AADriskMulti(mid, pid, nm)
+            m, p = O.Model(d["models"][mid]), O.Product(d["products"][pid])
+            _, ref = O.risk_multi(m, p, c["sobol"], c["npath"])  # exact path average
+            err = max(rel_to_max(r["values"], c["values"]), rel_to_max(r["risks"], ref))
+        worst[c["name"]] = err
+    bad = {k: v for k, v in worst.items() if not v < TOL}
+    assert not bad, bad
+
+
+def test_fp64_parity_large_vs_oracle(mc_eng):
+    # C2 shape (Dupire 60x30 UOC, 156 weekly steps, mrg32k3a) at 2^16 paths vs the oracle
+    eng, d = mc_eng
+    m, p = O.Model(d["models"]["dup60x30"]), O.Product(d["products"]["uoc"])
+    v, agg, ref = O.risk(m, p, 0, 1 << 16, np.array([1.0, 0.0]), fast=True, threads=8)
+    r = eng.AADriskOne("dup60x30", "uoc", num(0, 1 << 16))
+    assert rel_to_max(r["payoffValues"], v) < TOL
+    assert rel_to_max(r["risks"], ref) < TOL
+
+
+def test_determinism(mc_eng):
+    eng, _ = mc_eng
+    a = eng.AADriskOne("dup60x30", "uoc", num(0, 50000, "fp32"))
+    b = eng.AADriskOne("dup60x30", "uoc", num(0, 50000, "fp32"))
+    assert (a["risks"] == b["risks"]).all() and (a["payoffValues"] == b["payoffValues"]).all()
+
+
+def test_odd_and_tiny_path_counts(mc_eng):
+    eng, d = mc_eng
+    m, p = O.Model(d["models"]["dup20x10"]), O.Product(d["products"]["uoc"])
+    for n in (1, 2, 3, 31, 33, 1001):
+        for sob in (0, 1):
+            v, agg, ref = O.risk(m, p, sob, n, np.array([1.0, 0.0]))
+            r = eng.AADriskOne("dup20x10", "uoc", num(sob, n))
+            assert rel_to_max(r["payoffValues"], v) < TOL, (n, sob)
+            assert rel_to_max(r["risks"], ref) < TOL, (n, sob)
+
+
+@pytest.mark.parametrize("grid", [(20, 10), (60, 30), (120, 60)])
+def test_fp32_form_within_tenth_of_stderr(eng, grid):
+    """FP32 path arithmetic with exact accumulation vs the FP64 form on the same paths: every
+    price and every risk within 0.1 Monte Carlo standard error (spec tolerance)."""
+    from compfinance_gb300 import workloads as W
+    s, t, v = W.dupire_surface(*grid)
+    u = W.UOC_BARRIER
+    mid = f"eq{grid[0]}"
+    eng.putDupire(W.DUPIRE_SPOT, s, t, v, W.DUPIRE_MAXDT, mid)
+    eng.putBarrier(u["strike"], u["barrier"], u["maturity"], u["monitor_freq"], u["smooth"], 0, "equoc")
+    n = 1 << 18
+    # standard error of each risk at n paths, from 8 independent seed pairs at n/4 paths
+    rs = np.array([eng.AADriskOne(mid, "equoc", num(0, n // 4, "fp64", 1000 + k, 77 + k))["risks"]
+                   for k in range(8)])
+    se = rs.std(axis=0, ddof=1) / 2.0
+    for seeds in ((12345, 1234), (1001, 78), (4242, 99)):
+        r64 = eng.AADriskOne(mid, "equoc", num(0, n, "fp64", *seeds))
+        r32 = eng.AADriskOne(mid, "equoc", num(0, n, "fp32", *seeds))
+        v64 = eng.value(mid, "equoc", num(0, n, "fp64", *seeds))
+        assert np.all(np.abs(r32["payoffValues"] - r64["payoffValues"]) <= 0.1 * v64["stderrs"])
+        mask = se > 1e-6 * np.abs(r64["risks"]).max()
+        assert np.all(np.abs(r32["risks"] - r64["risks"])[mask] <= 0.1 * se[mask])
+        # nodes with no measurable variance must agree to FP32 rounding
+        assert np.all(np.abs(r32["risks"] - r64["risks"])[~mask] <= 1e-6 * np.abs(r64["risks"]).max())

@@ -210,7 +210,20 @@ class Engine:
             s.p[i] = x
         return s
 
-    def dupireCalib(self, ivs, inclSpots, maxDs, inclTimes, maxDtVol):
+    def dupireCalib(self, ivs, inclSpots, maxDs, inclTimes, maxDtVol, riskView=None):
+        """riskView = (strikes, mats, spreads[nK][nM]) shifts the implied vols (bump harness)."""
+        if riskView is not None:
+            a, b = _arr(inclSpots), _arr(inclTimes)
+            k, m, sp = _arr(riskView[0]), _arr(riskView[1]), _arr(riskView[2]).reshape(-1)
+            nS, nT = ctypes.c_int(), ctypes.c_int()
+            _check(lib().cf_dupire_calib(self._h, ctypes.byref(ivs), _p(a), len(a), ctypes.c_double(maxDs), _p(b),
+                                         len(b), ctypes.c_double(maxDtVol), ctypes.byref(nS), ctypes.byref(nT), None,
+                                         None, None))
+            s, t, lv = np.zeros(nS.value), np.zeros(nT.value), np.zeros(nS.value * nT.value)
+            _check(lib().cf_dupire_calib_view(self._h, ctypes.byref(ivs), _p(a), len(a), ctypes.c_double(maxDs), _p(b),
+                                              len(b), ctypes.c_double(maxDtVol), _p(k), len(k), _p(m), len(m), _p(sp),
+                                              ctypes.byref(nS), ctypes.byref(nT), _p(s), _p(t), _p(lv)))
+            return dict(spots=s, times=t, lVols=lv.reshape(nS.value, nT.value))
         a, b = _arr(inclSpots), _arr(inclTimes)
         nS, nT = ctypes.c_int(), ctypes.c_int()
         _check(lib().cf_dupire_calib(self._h, ctypes.byref(ivs), _p(a), len(a), ctypes.c_double(maxDs), _p(b), len(b),

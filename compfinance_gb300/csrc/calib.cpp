@@ -40,7 +40,8 @@ struct CalibRun
 // host, exactly as the reference decides them; the 5 calls per node and Dupire's formula on
 // the GPU.
 int calibrate(Context& c, const cf_ivs& ivs, const double* inclSpots, int nIS, double maxDs, const double* inclTimes,
-              int nIT, double maxDtVol, const double* rvK, int nK, const double* rvM, int nM, CalibRun& r)
+              int nIT, double maxDtVol, const double* rvK, int nK, const double* rvM, int nM, CalibRun& r,
+              const double* spreads = nullptr)
 {
     if (!inclSpots || !inclTimes || nIS < 1 || nIT < 1) return fail(CF_E_ARG, "dupireCalib: empty grid");
     if (ivs.kind != 0 && ivs.kind != 1) return fail(CF_E_ARG, "dupireCalib: unknown IVS kind");
@@ -64,7 +65,7 @@ int calibrate(Context& c, const cf_ivs& ivs, const double* inclSpots, int nIS, d
     }
     const size_t n5 = size_t(nS) * nT * 5;
     const size_t bytes = (nS + nT + nK + nM) * 8 + 2 * nT * 4 + 2 * n5 * 8 + size_t(nS) * nT * 16 +
-                         size_t(nK) * nM * 16 + 1024;
+                         size_t(nK) * nM * 24 + 4096;
     int rc = r.buf.ensure(bytes);
     if (rc) return rc;
     char* d = static_cast<char*>(r.buf.ptr);
@@ -95,6 +96,8 @@ int calibrate(Context& c, const cf_ivs& ivs, const double* inclSpots, int nIS, d
     double* dK = (double*)take(size_t(nK) * 8 + 8);
     double* dM = (double*)take(size_t(nM) * 8 + 8);
     P.acc = (long long*)take(size_t(nK) * nM * 16 + 16);
+    double* dSp = (double*)take(size_t(nK) * nM * 8 + 8);
+    P.spreads = spreads ? dSp : nullptr;
     P.spots = dS;
     P.times = dT;
     P.il = dil;
@@ -107,7 +110,8 @@ int calibrate(Context& c, const cf_ivs& ivs, const double* inclSpots, int nIS, d
         cudaMemcpyAsync(dil, r.il.data(), nT * 4, cudaMemcpyHostToDevice, s) ||
         cudaMemcpyAsync(dih, r.ih.data(), nT * 4, cudaMemcpyHostToDevice, s) ||
         (nK && cudaMemcpyAsync(dK, rvK, nK * 8, cudaMemcpyHostToDevice, s)) ||
-        (nM && cudaMemcpyAsync(dM, rvM, nM * 8, cudaMemcpyHostToDevice, s)))
+        (nM && cudaMemcpyAsync(dM, rvM, nM * 8, cudaMemcpyHostToDevice, s)) ||
+        (spreads && cudaMemcpyAsync(dSp, spreads, size_t(nK) * nM * 8, cudaMemcpyHostToDevice, s)))
         return cuda_fail(cudaGetLastError(), "calibration upload");
     rc = launch_calib(P, 0, s);
     if (rc) return cuda_fail(cudaError_t(rc), "calibration kernels");
@@ -138,6 +142,17 @@ int cf_dupire_calib(cf_context* ctx, const cf_ivs* ivs, const double* inclSpots,
                     const double* inclTimes, int nInclTimes, double maxDtVol, int* nS, int* nT, double* spots,
                     double* times, double* lvols)
 {
+    return cf_dupire_calib_view(ctx, ivs, inclSpots, nInclSpots, maxDs, inclTimes, nInclTimes, maxDtVol, nullptr, 0,
+                                nullptr, 0, nullptr, nS, nT, spots, times, lvols);
+}
+
+int cf_dupire_calib_view(cf_context* ctx, const cf_ivs* ivs, const double* inclSpots, int nInclSpots, double maxDs,
+                         const double* inclTimes, int nInclTimes, double maxDtVol, const double* rvStrikes,
+                         int nStrikes, const double* rvMats, int nMats, const double* spreads, int* nS, int* nT,
+                         double* spots, double* times, double* lvols)
+{
+    if (spreads && (!rvStrikes || !rvMats || nStrikes < 1 || nMats < 1))
+        return fail(CF_E_ARG, "dupireCalib: spreads need a risk view");
     if (!ctx || !ivs || !nS || !nT) return fail(CF_E_ARG, "null argument");
     std::lock_guard<std::mutex> lock(ctx->mu);
     cudaSetDevice(ctx->c.device);
@@ -150,8 +165,8 @@ int cf_dupire_calib(cf_context* ctx, const cf_ivs* ivs, const double* inclSpots,
         return CF_OK;
     }
     CalibRun r;
-    int rc = calibrate(ctx->c, *ivs, inclSpots, nInclSpots, maxDs, inclTimes, nInclTimes, maxDtVol, nullptr, 0,
-                       nullptr, 0, r);
+    int rc = calibrate(ctx->c, *ivs, inclSpots, nInclSpots, maxDs, inclTimes, nInclTimes, maxDtVol, rvStrikes,
+                       spreads ? nStrikes : 0, rvMats, spreads ? nMats : 0, r, spreads);
     if (rc) return rc;
     std::vector<double> lv;
     if ((rc = fetch_lvols(ctx->c, r, lv))) return rc;

@@ -105,6 +105,8 @@ __device__ __forceinline__ void fd_point(int pt, double K, double T, double& Kp,
     if (pt == 4) Kp = K + 1.0e-04;
 }
 
+__device__ int rv_weights(const CalibParams& p, double K, double T, int* node, double* w);
+
 __global__ void calib_points_kernel(CalibParams p)
 {
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
@@ -113,7 +115,16 @@ __global__ void calib_points_kernel(CalibParams p)
     if (i < p.il[j] || i > p.ih[j]) return;
     double Kp, Tp;
     fd_point(pt, p.spots[i], p.times[j], Kp, Tp);
-    const double vol = dimplied(p, Kp, Tp) + 0.0;  // risk view spreads are zero
+    double vol = dimplied(p, Kp, Tp);
+    if (p.spreads)  // IVS::call adds the risk view's smoothstep-interpolated spread (ivs.h:103-116)
+    {
+        int node[4];
+        double w[4];
+        const int n = rv_weights(p, Kp, Tp, node, w);
+        double sp = 0.0;
+        for (int q = 0; q < n; ++q) sp += w[q] * p.spreads[node[q]];
+        vol += sp;
+    }
     p.c[idx] = dbs(p.spot, Kp, vol, Tp);
     p.vega[idx] = dbs_vega(p.spot, Kp, vol, Tp);
 }

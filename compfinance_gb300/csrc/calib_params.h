@@ -20,6 +20,7 @@ struct CalibParams
     double* vega;     // [nT][nS][5] d call / d vol
     double* lvT;      // [nT][nS] local vols, maturity-major
     const double* seed;   // [nS][nT] adjoint of each local vol (extrapolation folded in)
+    const double* spreads;  // [nK][nM] risk-view spreads added to the implied vols, or null
     long long* acc;       // [nK*nM][2] fixed-point accumulators of d / d spread
 };
 

@@ -81,7 +81,7 @@ struct Context
     std::map<std::string, ModelDesc> models;
     std::map<std::string, ProductDesc> products;
     std::map<std::pair<std::string, std::string>, std::unique_ptr<Plan>> plans;
-    DevBuf jump, err, work, scratch;
+    DevBuf jump, err, work, scratch, multiBuf;
     const unsigned long long* jumpA = nullptr;
     const unsigned long long* jumpB = nullptr;
     std::vector<double> hostW;

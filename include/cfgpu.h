@@ -125,6 +125,14 @@ int cf_dupire_calib(cf_context* ctx, const cf_ivs* ivs, const double* inclSpots,
                     double maxDs, const double* inclTimes, int nInclTimes, double maxDtVol, int* nS, int* nT,
                     double* spots, double* times, double* lvols);
 
+/* dupireCalib with a risk view (ivs.h:27-81, the calibration of dupireSuperbucketBump,
+ * main.h:575-696): the implied vols are shifted by the view's spreads[nStrikes*nMats],
+ * smoothstep-interpolated in strike and maturity. */
+int cf_dupire_calib_view(cf_context* ctx, const cf_ivs* ivs, const double* inclSpots, int nInclSpots,
+                         double maxDs, const double* inclTimes, int nInclTimes, double maxDtVol,
+                         const double* rvStrikes, int nStrikes, const double* rvMats, int nMats,
+                         const double* spreads, int* nS, int* nT, double* spots, double* times, double* lvols);
+
 /* dupireSuperbucket, main.h:453-569: calibrate, Monte Carlo adjoints to the local vols
  * (microbucket), then the adjoint of the calibration to the risk view's implied-vol
  * spreads.  vega[nStrikes * nMats]; microbucket[nS * nT] optional.  refSeeding = 1

@@ -1,0 +1,183 @@
+"""AADriskMulti of a European portfolio, Dupire calibration, the superbucket, and
+finite-difference checks of the adjoints, on the GPU."""
+import numpy as np
+import pytest
+
+import oracle as O
+from compfinance_gb300 import Engine
+from compfinance_gb300 import workloads as W
+from gpu_util import num, rel_to_max
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def eng():
+    e = Engine(0)
+    yield e
+    e.close()
+
+
+@pytest.fixture(scope="module")
+def portfolio(eng):
+    mats, strikes = W.superbucket_portfolio(10, 20)
+    s, t, v = W.dupire_surface(60, 30)
+    eng.putDupire(100.0, s, t, v, 1.0 / 12.0, "c4dup")
+    eng.putEuropeans(mats, strikes, "c4port")
+    m = O.Model(dict(kind="dupire", spot=100.0, spots=s, times=t, vols=v, maxdt=1.0 / 12.0))
+    p = O.Product(dict(kind="europeans", mats=mats, strikes=strikes))
+    return m, p
+
+
+def test_multi_c4_shape_fp64_vs_oracle(eng, portfolio):
+    """200 payoffs x 1801 parameters, 36 monthly steps: exact per-payoff path averages."""
+    m, p = portfolio
+    for sob in (1, 0):
+        r = eng.AADriskMulti("c4dup", "c4port", num(sob, 2048))
+        v, ref = O.risk_multi(m, p, sob, 2048)
+        assert r["risks"].shape == (1801, 200)
+        assert rel_to_max(r["values"], v) < 1e-12
+        assert rel_to_max(r["risks"], ref) < 1e-12
+
+
+def test_multi_fp32_vs_fp64(eng, portfolio):
+    """FP32 paths vs FP64 on the same mrg32k3a paths: within 0.1 Monte Carlo standard error."""
+    n = 1 << 16
+    runs = np.array([eng.AADriskMulti("c4dup", "c4port", num(0, n // 4, "fp64", 3000 + k, 11 + k))["risks"]
+                     for k in range(8)])
+    se = runs.std(axis=0, ddof=1) / 2.0
+    r64 = eng.AADriskMulti("c4dup", "c4port", num(0, n))
+    r32 = eng.AADriskMulti("c4dup", "c4port", num(0, n, "fp32"))
+    vse = eng.value("c4dup", "c4port", num(0, n))["stderrs"]
+    assert np.all(np.abs(r32["values"] - r64["values"]) <= 0.1 * vse)
+    mask = se > 1e-6 * np.abs(r64["risks"]).max()
+    assert np.all(np.abs(r32["risks"] - r64["risks"])[mask] <= 0.1 * se[mask])
+    assert np.all(np.abs(r32["risks"] - r64["risks"])[~mask] <= 1e-6 * np.abs(r64["risks"]).max())
+
+
+def test_multi_matches_risk_one(eng, portfolio):
+    """Each column of AADriskMulti equals AADriskOne of that payoff on the same paths."""
+    labels = eng.payoffLabels("c4port")
+    r = eng.AADriskMulti("c4dup", "c4port", num(1, 4096))
+    for k in (0, 7, 55, 199):
+        one = eng.AADriskOne("c4dup", "c4port", num(1, 4096), labels[k])
+        assert rel_to_max(r["risks"][:, k], one["risks"]) < 1e-12
+
+
+def test_calibration_vs_reference(eng, golden):
+    """Local vols from Dupire's formula on Black-Scholes prices (ivs.h:119-138).
+
+    The formula divides a second strike difference of prices (step 1e-4) by 1e-8, so the
+    reference's own local vols carry rounding noise (~1e-4 relative near the money, ~1e-3 at
+    the +-2.5 std cut-off): ulp-level differences between CUDA's and glibc's exp/log show up
+    at that level.
+    """
+    for c in golden("calib")["calib"]:
+        iv = Engine.ivs(c["ivs"], c["ivs_params"][0], c["ivs_params"][1:])
+        r = eng.dupireCalib(iv, c["incl_spots"], c["max_ds"], c["incl_times"], c["max_dt_vol"])
+        assert list(r["spots"]) == c["spots"] and list(r["times"]) == c["times"]
+        ref = np.array(c["lvols"]).reshape(r["lVols"].shape)
+        rel = np.abs(r["lVols"] - ref) / np.abs(ref)
+        print(c["name"], "max", rel.max(), "median", np.median(rel))
+        assert rel.max() < 1e-2, c["name"]
+        assert np.median(rel) < 1e-3, c["name"]
+
+
+@pytest.mark.parametrize("which", ["sb_param", "sb_merton"])
+def test_superbucket_vs_reference_and_oracle(eng, golden, which):
+    c = [x for x in golden("calib")["superbucket"] if x["name"] == which][0]
+    iv = Engine.ivs(c["ivs"], c["ivs_params"][0], c["ivs_params"][1:])
+    eng.putEuropeans(c["portfolio"]["mats"], c["portfolio"]["strikes"], "sbport")
+    w = np.zeros(len(c["portfolio"]["mats"]))
+    for k, x in c["notionals"]:
+        w[k] = x
+    args = (iv, 100.0, c["maxdt"], "sbport", w, c["incl_spots"], c["max_ds"], c["incl_times"], c["max_dt_vol"],
+            c["rv_strikes"], c["rv_mats"], num(1, c["npath"]))
+    r = eng.dupireSuperbucket(*args, refSeeding=True)
+    # the local vols differ from the reference's by their rounding noise (see above)
+    print(which, r["value"] - c["value"], r["delta"] - c["delta"], rel_to_max(r["vega"], c["vega"]))
+    assert abs(r["value"] - c["value"]) < 1e-4 * abs(c["value"])
+    assert abs(r["delta"] - c["delta"]) < 1e-3 * abs(c["delta"])
+    assert rel_to_max(r["vega"], c["vega"]) < 5e-2
+    # the calibration adjoint alone, on the same microbucket, against the oracle's tape
+    ex = eng.dupireSuperbucket(*args, refSeeding=False)
+    oiv = O.ivs(c["ivs"], c["ivs_params"][0], c["ivs_params"][1:])
+    ovega = O.calib_adjoint(oiv, c["incl_spots"], c["max_ds"], c["incl_times"], c["max_dt_vol"], c["rv_strikes"],
+                            c["rv_mats"], ex["microbucket"])
+    print(which, "adjoint vs oracle", rel_to_max(ex["vega"], ovega))
+    assert rel_to_max(ex["vega"], ovega) < 5e-2
+
+
+def test_superbucket_finite_differences(eng):
+    """Superbucket vega against bump / recalibrate / reprice of 20 seeded risk-view nodes
+    (the reference's dupireSuperbucketBump, main.h:575-696), common random numbers."""
+    iv = Engine.ivs("param", 100.0, [W.SB_IVS["a"], W.SB_IVS["b"], W.SB_IVS["c"], W.SB_IVS["sref"]])
+    isp, mds, itm, mdt = W.superbucket_grid(30, 12)
+    rk, rm = W.superbucket_riskview(15, 6)
+    mats, strikes = W.superbucket_portfolio(5, 8)
+    eng.putEuropeans(mats, strikes, "fdport")
+    w = np.ones(len(mats))
+    nm = num(1, 1 << 14)
+    sb = eng.dupireSuperbucket(iv, 100.0, 1.0 / 12.0, "fdport", w, isp, mds, itm, mdt, rk, rm, nm)
+    rs = np.random.RandomState(2018)
+    nodes = [(rs.randint(len(rk)), rs.randint(len(rm))) for _ in range(20)]
+    h = 1e-2  # the recalibration's own rounding noise (~1e-4 of prices) swamps smaller bumps
+    worst = 0.0
+    scale = np.abs(sb["vega"]).max()
+    for (i, j) in nodes:
+        vals = []
+        for sgn in (1.0, -1.0):
+            sp = np.zeros((len(rk), len(rm)))
+            sp[i, j] = sgn * h
+            cal = eng.dupireCalib(iv, isp, mds, itm, mdt, riskView=(rk, rm, sp))
+            eng.putDupire(100.0, cal["spots"], cal["times"], cal["lVols"], 1.0 / 12.0, "fdmodel")
+            vals.append(eng.value("fdmodel", "fdport", nm)["values"] @ w)
+        fd = (vals[0] - vals[1]) / (2 * h)
+        worst = max(worst, abs(fd - sb["vega"][i, j]) / scale)
+    print("superbucket FD worst error / max vega", worst)
+    assert worst < 3e-2
+
+
+def test_risk_finite_differences(eng):
+    """AAD risks against central bumps on the same paths (common random numbers): spot on a
+    European call, 8 seeded local vols on the barrier.  (The barrier's smoothing width is
+    frozen at S0 * smooth, mcPrd.h:247, so its AAD spot risk deliberately omits
+    d smooth / d spot, which a bumped spot would include.)"""
+    s, t, v = W.dupire_surface(20, 10)
+    u = W.UOC_BARRIER
+    eng.putBarrier(u["strike"], u["barrier"], u["maturity"], u["monitor_freq"], u["smooth"], 0, "fduoc")
+    eng.putEuropean(110.0, 2.0, 2.0, "fdcall")
+    eng.putDupire(100.0, s, t, v, 0.25, "fdbase")
+    nm = num(0, 1 << 14)
+    rs = np.random.RandomState(7)
+    cases = [("fdcall", -1, -1)] + [("fduoc", rs.randint(4, 16), rs.randint(10)) for _ in range(8)]
+    for (prd, i, j) in cases:
+        r = eng.AADriskOne("fdbase", prd, nm)["risks"]
+        scale = np.abs(r).max()
+        vals = []
+        for sgn in (1.0, -1.0):
+            if i < 0:
+                h = 1e-4
+                eng.putDupire(100.0 + sgn * h, s, t, v, 0.25, "fdbump")
+            else:
+                h = 1e-5
+                vb = v.copy()
+                vb[i, j] += sgn * h
+                eng.putDupire(100.0, s, t, vb, 0.25, "fdbump")
+            vals.append(eng.value("fdbump", prd, nm)["values"][0])
+        fd = (vals[0] - vals[1]) / (2 * h)
+        aad = r[0] if i < 0 else r[1 + i * 10 + j]
+        assert abs(fd - aad) <= 2e-3 * abs(aad) + 1e-6 * scale, (prd, i, j, fd, aad)
+
+
+def test_superbucket_c4_shape(eng):
+    """C4 shape: 30x12 implied vols -> 60x30 local vols -> 200 Europeans, 36 monthly steps."""
+    iv = Engine.ivs("param", 100.0, [W.SB_IVS["a"], W.SB_IVS["b"], W.SB_IVS["c"], W.SB_IVS["sref"]])
+    isp, mds, itm, mdt = W.superbucket_grid(60, 30)
+    rk, rm = W.superbucket_riskview(30, 12)
+    mats, strikes = W.superbucket_portfolio(10, 20)
+    eng.putEuropeans(mats, strikes, "c4port2")
+    w = np.ones(len(mats))
+    r = eng.dupireSuperbucket(iv, 100.0, 1.0 / 12.0, "c4port2", w, isp, mds, itm, mdt, rk, rm, num(1, 1 << 16))
+    assert r["vega"].shape == (30, 12) and r["microbucket"].shape == (60, 30)
+    assert np.isfinite(r["vega"]).all() and r["value"] > 0

@@ -124,6 +124,31 @@ def cpu_baseline(seconds=12.0, threads=None):
             "sample": f"{n} paths of the same workload (FP64, hand-written adjoint), {dt:.2f} s"}
 
 
+def serving_leg(eng, n, seed):
+    """Mixed request stream (seeded Poisson arrivals at 2,000 req/s; 40% BS values, 40% Dupire
+    barrier risks of 2^16-2^20 paths on 20x10..120x60 grids with 12..520 steps, 20% European
+    portfolio AADriskMulti), FP32 path form, 64 GB admission budget, 8 slots; then the same
+    requests one at a time through the synchronous entry points."""
+    from compfinance_gb300.serve_stream import load_store, run_one_at_a_time, run_stream
+    models, products = W.serving_store()
+    load_store(eng, models, products)
+    stream = W.serving_stream(n=n, rate=2000.0, seed=seed)
+    for r in stream:  # lower every plan and warm each kernel variant before timing
+        eng.shapes(r["model"], r["product"])
+    run_stream(eng, W.serving_stream(n=64, rate=1e6, seed=seed + 1), slots=8)
+    stats, makespan, status, _ = run_stream(eng, stream, slots=8, budget=64 << 30)
+    t_seq, steps = run_one_at_a_time(eng, stream)
+    served = stats["pathStepsDone"] / makespan
+    batch = steps / t_seq
+    return {"requests": n, "arrival_rate_req_s": 2000.0, "slots": 8, "hbm_budget_gb": 64,
+            "completed": stats["completed"], "failed": stats["failed"], "rejected": stats["rejected"],
+            "p50_ms": stats["p50Ms"], "p99_ms": stats["p99Ms"], "mean_ms": stats["meanMs"],
+            "makespan_s": makespan, "served_path_steps_per_s": served,
+            "one_at_a_time_s": t_seq, "one_at_a_time_path_steps_per_s": batch,
+            "served_over_one_at_a_time": served / batch, "max_in_flight": stats["maxInFlight"],
+            "peak_footprint_gb": stats["peakFootprint"] / 2**30}
+
+
 def run_reference(args):
     rank, world, _ = env_rank()
     if rank != 0:
@@ -144,6 +169,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving-stream leg")
+    ap.add_argument("--serve-requests", type=int, default=10000)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -266,6 +293,8 @@ def main():
         "clocks": clocks,
         "step_ms": [round(x, 4) for x in ms32],
     }
+    if not args.no_serving:
+        out["serving"] = serving_leg(eng, args.serve_requests, seed=2026 + rank)
     if rank == 0 and not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline()
     if rank == 0:

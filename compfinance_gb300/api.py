@@ -294,3 +294,93 @@ class Engine:
         agg = ctypes.c_double()
         _check(lib().cf_fetch_result(self._h, _p(v), _p(e), ctypes.byref(agg), _p(r) if nparam else None))
         return v, e, agg.value, r[:nparam]
+
+
+class CfRequest(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int), ("modelId", ctypes.c_char_p), ("productId", ctypes.c_char_p),
+                ("num", CfNumParam), ("weights", _dp), ("nWeights", ctypes.c_int),
+                ("queueTimeoutMs", ctypes.c_double)]
+
+
+class CfServingStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_uint64), ("completed", ctypes.c_uint64), ("failed", ctypes.c_uint64),
+                ("rejected", ctypes.c_uint64), ("cancelled", ctypes.c_uint64), ("timedOut", ctypes.c_uint64),
+                ("p50Ms", ctypes.c_double), ("p99Ms", ctypes.c_double), ("meanMs", ctypes.c_double),
+                ("pathStepsDone", ctypes.c_uint64), ("maxInFlight", ctypes.c_int),
+                ("peakFootprint", ctypes.c_uint64)]
+
+
+STATUS = {0: "queued", 1: "running", 2: "done", 3: "failed", 4: "rejected", 5: "cancelled", 6: "timeout"}
+KINDS = {"value": 0, "risk": 1, "multi": 2}
+
+
+class Server:
+    """Continuous-batching server over an Engine: `slots` concurrent CUDA streams, admission
+    by device-memory footprint (hbm_budget bytes)."""
+
+    def __init__(self, engine, slots=8, hbm_budget=64 << 30):
+        self.eng = engine
+        h = ctypes.c_void_p()
+        _check(lib().cf_server_create(engine._h, int(slots), ctypes.c_uint64(hbm_budget), ctypes.byref(h)))
+        self._h = h
+        self._shape = {}
+
+    def close(self):
+        if self._h:
+            lib().cf_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, kind, modelId, productId, num, weights=None, queue_timeout_ms=0.0):
+        w = None if weights is None else _arr(weights)
+        r = CfRequest(KINDS[kind], modelId.encode(), productId.encode(), num.c(), None if w is None else _p(w),
+                      0 if w is None else len(w), float(queue_timeout_ms))
+        rid = ctypes.c_uint64()
+        _check(lib().cf_server_submit(self._h, ctypes.byref(r), ctypes.byref(rid)))
+        self._shape[rid.value] = (kind, modelId, productId)
+        return rid.value
+
+    def cancel(self, rid):
+        _check(lib().cf_server_cancel(self._h, ctypes.c_uint64(rid)))
+
+    def wait(self, rid, timeout_ms=-1):
+        st = ctypes.c_int()
+        _check(lib().cf_server_wait(self._h, ctypes.c_uint64(rid), int(timeout_ms), ctypes.byref(st)))
+        return STATUS[st.value]
+
+    def error(self):
+        buf = ctypes.create_string_buffer(4096)
+        lib().cf_last_error(buf, ctypes.c_size_t(4096))
+        return buf.value.decode(errors="replace")
+
+    def result(self, rid):
+        kind, mid, pid = self._shape[rid]
+        npay, npar, _ = self.eng.shapes(mid, pid)
+        v, e = np.zeros(npay), np.zeros(npay)
+        r = np.zeros(max(1, npar * (npay if kind == "multi" else 1)))
+        agg, lat = ctypes.c_double(), ctypes.c_double()
+        _check(lib().cf_server_result(self._h, ctypes.c_uint64(rid), _p(v), _p(e), ctypes.byref(agg),
+                                      _p(r) if kind != "value" else None, ctypes.byref(lat)))
+        out = dict(values=v, stderrs=e, aggregate=agg.value, latency_ms=lat.value)
+        if kind == "risk":
+            out["risks"] = r[:npar]
+        elif kind == "multi":
+            out["risks"] = r.reshape(npar, npay)
+        return out
+
+    def release(self, rid):
+        _check(lib().cf_server_release(self._h, ctypes.c_uint64(rid)))
+        self._shape.pop(rid, None)
+
+    def stats(self):
+        s = CfServingStats()
+        _check(lib().cf_server_stats(self._h, ctypes.byref(s)))
+        return {k: getattr(s, k) for k, _ in CfServingStats._fields_}
+
+    def inject_failures(self, n):
+        _check(lib().cf_server_inject_failures(self._h, int(n)))

@@ -239,7 +239,7 @@ int cf_dupire_superbucket(cf_context* ctx, const cf_ivs* ivs, double spot, doubl
     if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
     if (e != cudaSuccess) return cuda_fail(e, "superbucket fetch");
     for (int k = 0; k < nStrikes * nMats; ++k) vega[k] = fix_value_host(acc[2 * k], acc[2 * k + 1]);
-    c.launches = 4;
+    c.main.launches = 4;
     return CF_OK;
 }
 

@@ -73,6 +73,35 @@ void DevBuf::release()
     bytes = 0;
 }
 
+int PinnedBuf::ensure(size_t n)
+{
+    if (n <= bytes) return CF_OK;
+    release();
+    const size_t want = n + n / 4;
+    cudaError_t e = cudaMallocHost(&ptr, want);
+    if (e != cudaSuccess)
+    {
+        ptr = nullptr;
+        bytes = 0;
+        return cuda_fail(e, "cudaMallocHost");
+    }
+    bytes = want;
+    return CF_OK;
+}
+
+void PinnedBuf::release()
+{
+    if (ptr) cudaFreeHost(ptr);
+    ptr = nullptr;
+    bytes = 0;
+}
+
+Slot::~Slot()
+{
+    if (done) cudaEventDestroy(done);
+    if (ownsStream && stream) cudaStreamDestroy(stream);
+}
+
 // ------------------------------------------------------------------------------------
 // Products: timelines, deflines and labels (mcPrd.h:43-80, 149-211, 305-340).
 // ------------------------------------------------------------------------------------
@@ -403,7 +432,7 @@ int Context::init(int dev)
     CF_CUDA(cudaMemcpy(static_cast<char*>(jump.ptr) + sizeof(A), B, sizeof(B), cudaMemcpyHostToDevice));
     jumpA = static_cast<const unsigned long long*>(jump.ptr);
     jumpB = jumpA + 64 * 9;
-    if ((rc = err.ensure(16))) return rc;
+    main.stream = stream;
     return CF_OK;
 }
 
@@ -437,8 +466,11 @@ int Context::getPlan(const std::string& mid, const std::string& pid, Plan*& out)
     return CF_OK;
 }
 
-// Enqueue one value (risk = false) or risk (risk = true, weights[nPay]) run.
-int Context::enqueue(Plan& plan, const cf_num_param& num, bool risk, const double* weights)
+// Enqueue one value (risk = false) or risk (risk = true, weights[nPay]) run on a slot: the
+// weights upload, the accumulator reset, the kernel and the download of the accumulators
+// into the slot's pinned buffer are all asynchronous on the slot's stream; slot.done is
+// recorded after them.
+int Context::enqueue(Slot& slot, Plan& plan, const cf_num_param& num, bool risk, const double* weights)
 {
     if (num.numPath <= 0) return fail(CF_E_ARG, "numPath must be positive");
     const bool sobol = num.useSobol != 0;
@@ -446,6 +478,7 @@ int Context::enqueue(Plan& plan, const cf_num_param& num, bool risk, const doubl
         return fail(CF_E_SHAPE, "Sobol dimension " + std::to_string(plan.nSteps) + " exceeds the " +
                                     std::to_string(sobol_max_dim()) + " dimensions of the direction numbers");
     const bool fp32 = num.precision == CF_FP32;
+    cudaStream_t st = slot.stream;
     McParams p = plan.base;
     p.nPath = num.numPath;
     p.seed1 = unsigned(num.seed1);
@@ -454,31 +487,28 @@ int Context::enqueue(Plan& plan, const cf_num_param& num, bool risk, const doubl
     p.mrgJumpB = jumpB;
     p.nRisk = risk ? plan.nParam : 0;
     p.nAcc = p.nRisk + 2 * plan.nPay + 2;
-    // weights (double and float copies) and accumulators share one buffer
+    // weights (double and float copies), accumulators and the error flag share one buffer
     const size_t wBytes = ((size_t(plan.nPay) * 12 + 255) & ~size_t(255));
     const size_t accBytes = size_t(p.nAcc) * 16;
-    int rc = work.ensure(wBytes + accBytes);
+    int rc = slot.work.ensure(wBytes + accBytes + 256);
     if (rc) return rc;
-    hostW.assign(size_t(plan.nPay) * 3, 0);
-    std::vector<double> wd(plan.nPay, 0.0);
-    std::vector<float> wf(plan.nPay, 0.0f);
-    if (weights)
-        for (int k = 0; k < plan.nPay; ++k)
-        {
-            wd[k] = weights[k];
-            wf[k] = float(weights[k]);
-        }
-    char* wbase = static_cast<char*>(work.ptr);
-    CF_CUDA(cudaMemcpyAsync(wbase, wd.data(), wd.size() * 8, cudaMemcpyHostToDevice, stream));
-    CF_CUDA(cudaMemcpyAsync(wbase + size_t(plan.nPay) * 8, wf.data(), wf.size() * 4, cudaMemcpyHostToDevice,
-                            stream));
-    h2d += wd.size() * 12;
+    if ((rc = slot.hostAcc.ensure(accBytes + 16))) return rc;
+    if ((rc = slot.hostW.ensure(size_t(plan.nPay) * 12 + 16))) return rc;
+    double* wd = static_cast<double*>(slot.hostW.ptr);
+    float* wf = reinterpret_cast<float*>(wd + plan.nPay);
+    for (int k = 0; k < plan.nPay; ++k)
+    {
+        wd[k] = weights ? weights[k] : 0.0;
+        wf[k] = float(wd[k]);
+    }
+    char* wbase = static_cast<char*>(slot.work.ptr);
+    CF_CUDA(cudaMemcpyAsync(wbase, wd, size_t(plan.nPay) * 12, cudaMemcpyHostToDevice, st));
+    h2d += size_t(plan.nPay) * 12;
     p.w = reinterpret_cast<const double*>(wbase);
     p.wf = reinterpret_cast<const float*>(wbase + size_t(plan.nPay) * 8);
     p.acc = reinterpret_cast<long long*>(wbase + wBytes);
-    p.err = static_cast<int*>(err.ptr);
-    CF_CUDA(cudaMemsetAsync(p.acc, 0, accBytes, stream));
-    CF_CUDA(cudaMemsetAsync(p.err, 0, 4, stream));
+    p.err = reinterpret_cast<int*>(wbase + wBytes + accBytes);
+    CF_CUDA(cudaMemsetAsync(p.acc, 0, accBytes + 16, st));
 
     McLaunch l{plan.model, plan.prod, sobol ? RNG_SOBOL : RNG_MRG, fp32 ? 1 : 0, risk ? 1 : 0, 0, 0, 0};
     // Shared-memory staging of the interpolated local vols (a bulk copy through the TMA
@@ -525,29 +555,49 @@ int Context::enqueue(Plan& plan, const cf_num_param& num, bool risk, const doubl
         p.scratchThreads = grid * 128;
         const size_t bytes = size_t(p.scratchFields) * size_t(plan.nSteps + 1) * size_t(p.scratchThreads) *
                              (fp32 ? 4 : 8);
-        if ((rc = scratch.ensure(bytes))) return rc;
-        p.scratch = scratch.ptr;
+        if ((rc = slot.scratch.ensure(bytes))) return rc;
+        p.scratch = slot.scratch.ptr;
     }
-    rc = launch_mc(l, p, stream);
+    rc = launch_mc(l, p, st);
     if (rc) return cuda_fail(cudaError_t(rc), "mc_kernel launch");
-    last = p;
-    lastLaunch = l;
-    lastPlan = &plan;
-    lastRisk = risk;
-    launches = 1;
+    CF_CUDA(cudaMemcpyAsync(slot.hostAcc.ptr, p.acc, accBytes + 16, cudaMemcpyDeviceToHost, st));
+    d2h += accBytes + 16;
+    if (!slot.done) CF_CUDA(cudaEventCreateWithFlags(&slot.done, cudaEventDisableTiming));
+    CF_CUDA(cudaEventRecord(slot.done, st));
+    slot.last = p;
+    slot.plan = &plan;
+    slot.risk = risk;
+    slot.multi = false;
+    slot.launches = 1;
     return CF_OK;
 }
 
-int Context::fetch(double* values, double* stderrs, double* aggregate, double* risks)
+// Estimated device footprint of a run (scratch of the reverse sweep + accumulators), the
+// admission currency of the serving loop.
+size_t Context::footprint(const Plan& plan, const cf_num_param& num, bool risk) const
 {
-    if (!lastPlan) return fail(CF_E_ARG, "nothing enqueued");
-    const McParams& p = last;
-    std::vector<long long> acc(size_t(p.nAcc) * 2);
-    int e = 0;
-    CF_CUDA(cudaMemcpyAsync(acc.data(), p.acc, acc.size() * 8, cudaMemcpyDeviceToHost, stream));
-    CF_CUDA(cudaMemcpyAsync(&e, p.err, 4, cudaMemcpyDeviceToHost, stream));
-    CF_CUDA(cudaStreamSynchronize(stream));
-    d2h += acc.size() * 8 + 4;
+    const bool sobol = num.useSobol != 0, fp32 = num.precision == CF_FP32;
+    const long long threads = std::min<long long>(sobol ? (num.numPath / 32 + 1) * 32 : (num.numPath + 1) / 2,
+                                                  (long long)numSMs * 16 * 128);
+    const int NP = sobol ? 1 : 2;
+    size_t b = size_t(plan.nParam + 2 * plan.nPay + 2) * 16 + size_t(plan.nPay) * 12 + 4096;
+    if (risk) b += size_t(1 + 3 * NP) * size_t(plan.nSteps + 1) * size_t(threads) * (fp32 ? 4 : 8);
+    return b;
+}
+
+bool Context::ready(Slot& slot) const
+{
+    return !slot.done || cudaEventQuery(slot.done) != cudaErrorNotReady;
+}
+
+int Context::fetch(Slot& slot, double* values, double* stderrs, double* aggregate, double* risks)
+{
+    if (!slot.plan) return fail(CF_E_ARG, "nothing enqueued");
+    CF_CUDA(cudaEventSynchronize(slot.done));
+    if (slot.multi) return finishMulti(slot, values, risks);
+    const McParams& p = slot.last;
+    const long long* acc = static_cast<const long long*>(slot.hostAcc.ptr);
+    const int e = *reinterpret_cast<const int*>(acc + 2 * size_t(p.nAcc));
     if (e) return fail(CF_E_DEVICE, "kernel error flag " + std::to_string(e));
     const double n = double(p.nPath);
     auto val = [&](int i) { return fix_value_host(acc[2 * size_t(i)], acc[2 * size_t(i) + 1]); };
@@ -559,8 +609,7 @@ int Context::fetch(double* values, double* stderrs, double* aggregate, double* r
         if (stderrs) stderrs[k] = std::sqrt(std::max(0.0, q / n - mean * mean) / n);
     }
     if (aggregate) aggregate[0] = val(p.nRisk + 2 * p.nPay) / n;
-    if (aggregate && stderrs == nullptr) {}
-    if (risks && lastRisk)
+    if (risks && slot.risk)
         for (int j = 0; j < p.nRisk; ++j) risks[j] = val(j) / n;
     return CF_OK;
 }
@@ -612,6 +661,7 @@ int cf_set_stream(cf_context* ctx, void* stream)
 {
     CF_CTX();
     ctx->c.stream = stream ? static_cast<cudaStream_t>(stream) : ctx->c.ownStream;
+    ctx->c.main.stream = ctx->c.stream;
     return CF_OK;
 }
 
@@ -844,7 +894,7 @@ int cf_enqueue(cf_context* ctx, const char* modelId, const char* productId, cons
         weights = w.data();
     }
     if ((rc = ctx->c.enqueue(*plan, *num, risk != 0, weights))) return rc;
-    if (launches) *launches = ctx->c.launches;
+    if (launches) *launches = ctx->c.main.launches;
     return CF_OK;
 }
 

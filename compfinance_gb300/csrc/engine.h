@@ -71,6 +71,42 @@ struct Plan
     McParams base;
 };
 
+// Pinned host memory (results are copied into it asynchronously).
+struct PinnedBuf
+{
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    int ensure(size_t n);
+    void release();
+    PinnedBuf() = default;
+    PinnedBuf(const PinnedBuf&) = delete;
+    PinnedBuf& operator=(const PinnedBuf&) = delete;
+    ~PinnedBuf() { release(); }
+};
+
+// Everything one in-flight run needs: its stream, device buffers, pinned result staging and
+// a completion event.  The synchronous API uses the context's main slot; the serving loop
+// owns several so that admitted requests overlap on the device.
+struct Slot
+{
+    cudaStream_t stream = nullptr;
+    bool ownsStream = false;
+    DevBuf work, scratch, multiBuf;
+    PinnedBuf hostAcc, hostW;
+    cudaEvent_t done = nullptr;
+    McParams last;
+    Plan* plan = nullptr;
+    bool risk = false, multi = false;
+    int launches = 0;
+    // multi-risk bookkeeping (strike buckets, see multi.cpp)
+    std::vector<int> evOff, orig;
+    std::vector<double> ks;
+    int multiParams = 0;
+    long long multiPaths = 0;
+    size_t accRBytes = 0, accVBytes = 0;
+    ~Slot();
+};
+
 struct Context
 {
     int device = 0;
@@ -81,25 +117,36 @@ struct Context
     std::map<std::string, ModelDesc> models;
     std::map<std::string, ProductDesc> products;
     std::map<std::pair<std::string, std::string>, std::unique_ptr<Plan>> plans;
-    DevBuf jump, err, work, scratch, multiBuf;
+    DevBuf jump;
     const unsigned long long* jumpA = nullptr;
     const unsigned long long* jumpB = nullptr;
-    std::vector<double> hostW;
-    // last enqueued run
-    McParams last;
-    McLaunch lastLaunch;
-    Plan* lastPlan = nullptr;
-    bool lastRisk = false;
-    int launches = 0;
+    Slot main;
     unsigned long long h2d = 0, d2h = 0;  // cumulative transfer bytes
 
     int init(int dev);
     ~Context();
     int getPlan(const std::string& mid, const std::string& pid, Plan*& out);
     int buildPlan(const ModelDesc& m, const ProductDesc& pd, Plan& plan);
-    int enqueue(Plan& plan, const cf_num_param& num, bool risk, const double* weights);
-    int fetch(double* values, double* stderrs, double* aggregate, double* risks);
+    const ProductDesc* productOf(const Plan& plan) const;
+    int enqueue(Slot& slot, Plan& plan, const cf_num_param& num, bool risk, const double* weights);
+    int fetch(Slot& slot, double* values, double* stderrs, double* aggregate, double* risks);
+    bool ready(Slot& slot) const;
+    size_t footprint(const Plan& plan, const cf_num_param& num, bool risk) const;
+    // AADriskMulti: the multi kernel (European portfolios) is asynchronous like enqueue
+    bool multiFast(const Plan& plan) const;
+    int enqueueMulti(Slot& slot, Plan& plan, const cf_num_param& num);
+    int finishMulti(Slot& slot, double* values, double* risks);
     int riskMulti(Plan& plan, const cf_num_param& num, double* values, double* risks);
+    // main-slot conveniences of the synchronous API
+    int enqueue(Plan& plan, const cf_num_param& num, bool risk, const double* weights)
+    {
+        main.stream = stream;
+        return enqueue(main, plan, num, risk, weights);
+    }
+    int fetch(double* values, double* stderrs, double* aggregate, double* risks)
+    {
+        return fetch(main, values, stderrs, aggregate, risks);
+    }
 };
 
 }  // namespace cf

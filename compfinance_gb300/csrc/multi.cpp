@@ -30,34 +30,31 @@ int launch_multi(int model, int rng, int fp32, int grid, size_t smem, const Mult
 
 constexpr int kMultiMaxE = 16;
 
-int Context::riskMulti(Plan& plan, const cf_num_param& num, double* values, double* risks)
+const ProductDesc* Context::productOf(const Plan& plan) const
 {
-    const ProductDesc* pd = nullptr;
     for (auto& kv : products)
-        if (kv.second.version == plan.pver) pd = &kv.second;
-    if (plan.prod != PROD_EUROPEANS || plan.nEv > kMultiMaxE || !pd)
-    {
-        std::vector<double> w(plan.nPay, 0.0), r(plan.nParam);
-        for (int k = 0; k < plan.nPay; ++k)
-        {
-            std::fill(w.begin(), w.end(), 0.0);
-            w[k] = 1.0;
-            int rc = enqueue(plan, num, true, w.data());
-            if (rc) return rc;
-            rc = fetch(k == 0 ? values : nullptr, nullptr, nullptr, r.data());
-            if (rc) return rc;
-            for (int j = 0; j < plan.nParam; ++j) risks[size_t(j) * plan.nPay + k] = r[j];
-        }
-        launches = plan.nPay;
-        return CF_OK;
-    }
+        if (kv.second.version == plan.pver) return &kv.second;
+    return nullptr;
+}
+
+bool Context::multiFast(const Plan& plan) const
+{
+    return plan.prod == PROD_EUROPEANS && plan.nEv <= kMultiMaxE && productOf(plan) != nullptr;
+}
+
+int Context::enqueueMulti(Slot& slot, Plan& plan, const cf_num_param& num)
+{
+    const ProductDesc* pd = productOf(plan);
+    if (!multiFast(plan)) return fail(CF_E_UNSUPPORTED, "multi kernel: European portfolios of <= 16 maturities");
     if (num.numPath <= 0) return fail(CF_E_ARG, "numPath must be positive");
     const bool sobol = num.useSobol != 0, fp32 = num.precision == CF_FP32;
     if (sobol && !plan.sobolOk) return fail(CF_E_SHAPE, "Sobol dimension exceeds the direction numbers");
+    cudaStream_t st = slot.stream;
     // strikes of each maturity sorted; payoff index of each sorted position
     const int nEv = plan.nEv;
-    std::vector<int> evOff(nEv + 1, 0), orig;
-    std::vector<double> ks;
+    slot.evOff.assign(nEv + 1, 0);
+    slot.orig.clear();
+    slot.ks.clear();
     for (int e = 0; e < nEv; ++e)
     {
         const int k0 = pd->payOff[e], k1 = pd->payOff[e + 1];
@@ -66,29 +63,39 @@ int Context::riskMulti(Plan& plan, const cf_num_param& num, double* values, doub
         std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return pd->kflat[a] < pd->kflat[b]; });
         for (int k : idx)
         {
-            orig.push_back(k);
-            ks.push_back(pd->kflat[k]);
+            slot.orig.push_back(k);
+            slot.ks.push_back(pd->kflat[k]);
         }
-        evOff[e + 1] = evOff[e] + (k1 - k0) + 1;
+        slot.evOff[e + 1] = slot.evOff[e] + (k1 - k0) + 1;
     }
-    const int nBuckets = evOff[nEv];
+    const int nBuckets = slot.evOff[nEv];
     const int nParam = plan.model == MODEL_BS ? 8 : plan.nParam;  // BS: (a, b) per parameter
-    std::vector<float> ksf(ks.begin(), ks.end());
-    const size_t offKs = 256 * ((evOff.size() * 4 + 255) / 256);
-    const size_t offKsf = offKs + 256 * ((ks.size() * 8 + 255) / 256);
-    const size_t offAccR = offKsf + 256 * ((ksf.size() * 4 + 255) / 256);
-    const size_t accRBytes = size_t(nBuckets) * nParam * 16, accVBytes = size_t(nBuckets) * 5 * 16;
-    const size_t offAccV = offAccR + 256 * ((accRBytes + 255) / 256);
-    int rc = multiBuf.ensure(offAccV + accVBytes);
+    std::vector<float> ksf(slot.ks.begin(), slot.ks.end());
+    auto up = [](size_t n) { return 256 * ((n + 255) / 256); };
+    const size_t offKs = up(slot.evOff.size() * 4);
+    const size_t offKsf = offKs + up(slot.ks.size() * 8);
+    const size_t offAccR = offKsf + up(ksf.size() * 4);
+    slot.accRBytes = size_t(nBuckets) * nParam * 16;
+    slot.accVBytes = size_t(nBuckets) * 5 * 16;
+    const size_t offAccV = offAccR + up(slot.accRBytes);
+    const size_t offErr = offAccV + up(slot.accVBytes);
+    int rc = slot.multiBuf.ensure(offErr + 256);
     if (rc) return rc;
-    char* d = static_cast<char*>(multiBuf.ptr);
-    cudaError_t e = cudaMemcpyAsync(d, evOff.data(), evOff.size() * 4, cudaMemcpyHostToDevice, stream);
-    if (!e) e = cudaMemcpyAsync(d + offKs, ks.data(), ks.size() * 8, cudaMemcpyHostToDevice, stream);
-    if (!e) e = cudaMemcpyAsync(d + offKsf, ksf.data(), ksf.size() * 4, cudaMemcpyHostToDevice, stream);
-    if (!e) e = cudaMemsetAsync(d + offAccR, 0, offAccV + accVBytes - offAccR, stream);
-    if (!e) e = cudaMemsetAsync(err.ptr, 0, 4, stream);
+    if ((rc = slot.hostAcc.ensure(slot.accRBytes + slot.accVBytes + 16))) return rc;
+    if ((rc = slot.hostW.ensure(slot.evOff.size() * 4 + slot.ks.size() * 12 + 64))) return rc;
+    char* hw = static_cast<char*>(slot.hostW.ptr);
+    std::memcpy(hw, slot.evOff.data(), slot.evOff.size() * 4);
+    std::memcpy(hw + slot.evOff.size() * 4, slot.ks.data(), slot.ks.size() * 8);
+    std::memcpy(hw + slot.evOff.size() * 4 + slot.ks.size() * 8, ksf.data(), ksf.size() * 4);
+    char* d = static_cast<char*>(slot.multiBuf.ptr);
+    cudaError_t e = cudaMemcpyAsync(d, hw, slot.evOff.size() * 4, cudaMemcpyHostToDevice, st);
+    if (!e) e = cudaMemcpyAsync(d + offKs, hw + slot.evOff.size() * 4, slot.ks.size() * 8, cudaMemcpyHostToDevice, st);
+    if (!e)
+        e = cudaMemcpyAsync(d + offKsf, hw + slot.evOff.size() * 4 + slot.ks.size() * 8, ksf.size() * 4,
+                            cudaMemcpyHostToDevice, st);
+    if (!e) e = cudaMemsetAsync(d + offAccR, 0, offErr + 16 - offAccR, st);
     if (e) return cuda_fail(e, "multi upload");
-    h2d += evOff.size() * 4 + ks.size() * 12;
+    h2d += slot.evOff.size() * 4 + slot.ks.size() * 12;
 
     MultiParams mp;
     mp.p = plan.base;
@@ -98,7 +105,7 @@ int Context::riskMulti(Plan& plan, const cf_num_param& num, double* values, doub
     p.seed2 = unsigned(num.seed2);
     p.mrgJumpA = jumpA;
     p.mrgJumpB = jumpB;
-    p.err = static_cast<int*>(err.ptr);
+    p.err = reinterpret_cast<int*>(d + offErr);
     mp.nParam = nParam;
     mp.evOff = reinterpret_cast<const int*>(d);
     mp.ksD = reinterpret_cast<const double*>(d + offKs);
@@ -120,42 +127,56 @@ int Context::riskMulti(Plan& plan, const cf_num_param& num, double* values, doub
     {
         p.scratchThreads = grid * 128;
         p.scratchFields = 1 + 3 * NP;
-        if ((rc = scratch.ensure(size_t(perThread) * p.scratchThreads * (fp32 ? 4 : 8)))) return rc;
-        p.scratch = scratch.ptr;
+        if ((rc = slot.scratch.ensure(size_t(perThread) * p.scratchThreads * (fp32 ? 4 : 8)))) return rc;
+        p.scratch = slot.scratch.ptr;
     }
-    rc = launch_multi(plan.model, sobol, fp32, int(grid), smem, mp, stream);
+    rc = launch_multi(plan.model, sobol, fp32, int(grid), smem, mp, st);
     if (rc) return cuda_fail(cudaError_t(rc), "multi kernel launch");
-    launches = 1;
+    char* ha = static_cast<char*>(slot.hostAcc.ptr);
+    e = cudaMemcpyAsync(ha, mp.accRisk, slot.accRBytes, cudaMemcpyDeviceToHost, st);
+    if (!e) e = cudaMemcpyAsync(ha + slot.accRBytes, mp.accVal, slot.accVBytes, cudaMemcpyDeviceToHost, st);
+    if (!e) e = cudaMemcpyAsync(ha + slot.accRBytes + slot.accVBytes, p.err, 4, cudaMemcpyDeviceToHost, st);
+    if (!e && !slot.done) e = cudaEventCreateWithFlags(&slot.done, cudaEventDisableTiming);
+    if (!e) e = cudaEventRecord(slot.done, st);
+    if (e) return cuda_fail(e, "multi download");
+    d2h += slot.accRBytes + slot.accVBytes + 4;
+    slot.plan = &plan;
+    slot.multi = true;
+    slot.risk = true;
+    slot.multiParams = nParam;
+    slot.multiPaths = num.numPath;
+    slot.launches = 1;
+    return CF_OK;
+}
 
-    std::vector<long long> accR(accRBytes / 8), accV(accVBytes / 8);
-    int flag = 0;
-    e = cudaMemcpyAsync(accR.data(), mp.accRisk, accRBytes, cudaMemcpyDeviceToHost, stream);
-    if (!e) e = cudaMemcpyAsync(accV.data(), mp.accVal, accVBytes, cudaMemcpyDeviceToHost, stream);
-    if (!e) e = cudaMemcpyAsync(&flag, err.ptr, 4, cudaMemcpyDeviceToHost, stream);
-    if (!e) e = cudaStreamSynchronize(stream);
-    if (e) return cuda_fail(e, "multi fetch");
-    d2h += accRBytes + accVBytes + 4;
+int Context::finishMulti(Slot& slot, double* values, double* risks)
+{
+    const Plan& plan = *slot.plan;
+    const char* ha = static_cast<const char*>(slot.hostAcc.ptr);
+    const long long* accR = reinterpret_cast<const long long*>(ha);
+    const long long* accV = reinterpret_cast<const long long*>(ha + slot.accRBytes);
+    const int flag = *reinterpret_cast<const int*>(ha + slot.accRBytes + slot.accVBytes);
     if (flag) return fail(CF_E_DEVICE, "kernel error flag " + std::to_string(flag));
-
     // suffix sums over buckets m > j for each sorted strike j
-    const double n = double(num.numPath);
-    auto V = [&](const std::vector<long long>& a, size_t i) { return fix_value_host(a[2 * i], a[2 * i + 1]); };
-    const int nP = plan.nParam;
+    const double n = double(slot.multiPaths);
+    auto V = [](const long long* a, size_t i) { return fix_value_host(a[2 * i], a[2 * i + 1]); };
+    const int nParam = slot.multiParams, nP = plan.nParam, nEv = plan.nEv;
     std::vector<double> sumR(nParam), sumV(5);
     int sorted = 0;
     for (int ev = 0; ev < nEv; ++ev)
     {
-        const int nK = evOff[ev + 1] - evOff[ev] - 1;
+        const int nK = slot.evOff[ev + 1] - slot.evOff[ev] - 1;
         std::fill(sumR.begin(), sumR.end(), 0.0);
         std::fill(sumV.begin(), sumV.end(), 0.0);
         for (int j = nK - 1; j >= 0; --j)
         {
-            const int bk = evOff[ev] + j + 1;  // bucket m = j + 1 pays strikes 0..j
+            const int bk = slot.evOff[ev] + j + 1;  // bucket m = j + 1 pays strikes 0..j
             for (int q = 0; q < 5; ++q) sumV[q] += V(accV, size_t(bk) * 5 + q);
             for (int q = 0; q < nParam; ++q) sumR[q] += V(accR, size_t(bk) * nParam + q);
-            const double K = ks[sorted + j];
-            const int k = orig[sorted + j];
+            const double K = slot.ks[sorted + j];
+            const int k = slot.orig[sorted + j];
             if (values) values[k] = (sumV[1] - K * sumV[0]) / n;
+            if (!risks) continue;
             if (plan.model == MODEL_BS)
                 for (int q = 0; q < 4; ++q) risks[size_t(q) * plan.nPay + k] = (sumR[2 * q] - K * sumR[2 * q + 1]) / n;
             else
@@ -163,6 +184,30 @@ int Context::riskMulti(Plan& plan, const cf_num_param& num, double* values, doub
         }
         sorted += nK;
     }
+    return CF_OK;
+}
+
+int Context::riskMulti(Plan& plan, const cf_num_param& num, double* values, double* risks)
+{
+    main.stream = stream;
+    if (multiFast(plan))
+    {
+        int rc = enqueueMulti(main, plan, num);
+        if (rc) return rc;
+        return fetch(main, values, nullptr, nullptr, risks);
+    }
+    std::vector<double> w(plan.nPay, 0.0), r(plan.nParam);
+    for (int k = 0; k < plan.nPay; ++k)
+    {
+        std::fill(w.begin(), w.end(), 0.0);
+        w[k] = 1.0;
+        int rc = enqueue(plan, num, true, w.data());
+        if (rc) return rc;
+        rc = fetch(k == 0 ? values : nullptr, nullptr, nullptr, r.data());
+        if (rc) return rc;
+        for (int j = 0; j < plan.nParam; ++j) risks[size_t(j) * plan.nPay + k] = r[j];
+    }
+    main.launches = plan.nPay;
     return CF_OK;
 }
 

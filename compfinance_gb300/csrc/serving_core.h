@@ -1,0 +1,205 @@
+// Slot scheduler of the serving loop (continuous batching).
+//
+// Requests are admitted in arrival order into a fixed set of execution slots, each with its
+// own CUDA stream, under a device-memory budget: a request starts as soon as a slot is free
+// and its footprint fits the memory left, so work that arrives while other requests are on
+// the GPU overlaps with them.  Finished slots are reaped by polling; queued requests can be
+// cancelled or expire after their queue timeout; a request whose footprint exceeds the whole
+// budget is rejected at submission.  The executor does the work; it is a template parameter
+// so that the admission logic is tested on the CPU with a fake executor.
+//
+// Executor interface:
+//   int  start(Job& job, int slot)    0, or an error code (the job fails, the slot is freed)
+//   bool poll(int slot)               true once the slot's work has completed
+//   int  finish(Job& job, int slot)   0, or an error code (the job fails)
+//   std::string error()               message of the last failure
+#pragma once
+
+#include <algorithm>
+#include <cstdint>
+#include <deque>
+#include <map>
+#include <string>
+#include <vector>
+
+namespace cf {
+namespace serve {
+
+enum Status : int { QUEUED = 0, RUNNING = 1, DONE = 2, FAILED = 3, REJECTED = 4, CANCELLED = 5, TIMEOUT = 6 };
+
+struct Job
+{
+    uint64_t id = 0;
+    int status = QUEUED;
+    int slot = -1;
+    size_t footprint = 0;
+    double tSubmit = 0, tStart = 0, tDone = 0;
+    double queueTimeout = 0;  // seconds a request may wait for a slot (0 = no limit)
+    std::string error;
+    long long work = 0;       // path-steps, for throughput accounting
+};
+
+template <class Exec>
+class Scheduler
+{
+public:
+    Scheduler(Exec& ex, int nSlots, size_t budget) : ex_(ex), slots_(nSlots, 0), budget_(budget) {}
+
+    // Registers a request; a request larger than the whole budget is rejected at once.
+    uint64_t submit(size_t footprint, double queueTimeout, double now, long long work = 0)
+    {
+        Job j;
+        j.id = ++nextId_;
+        j.footprint = footprint;
+        j.tSubmit = now;
+        j.queueTimeout = queueTimeout;
+        j.work = work;
+        if (footprint > budget_)
+        {
+            j.status = REJECTED;
+            j.error = "request footprint " + std::to_string(footprint) + " B exceeds the device budget " +
+                      std::to_string(budget_) + " B";
+            j.tDone = now;
+            ++rejected_;
+        }
+        else
+            queue_.push_back(j.id);
+        jobs_[j.id] = j;
+        ++submitted_;
+        return j.id;
+    }
+
+    // Cancels a request that has not started yet.
+    bool cancel(uint64_t id, double now)
+    {
+        auto it = jobs_.find(id);
+        if (it == jobs_.end() || it->second.status != QUEUED) return false;
+        it->second.status = CANCELLED;
+        it->second.tDone = now;
+        queue_.erase(std::remove(queue_.begin(), queue_.end(), id), queue_.end());
+        ++cancelled_;
+        return true;
+    }
+
+    // One scheduling round: reap finished slots, expire queue time-outs, admit in arrival
+    // order while a slot is free and the head request fits the memory left.  Returns the
+    // number of state changes (0 = nothing happened).
+    int step(double now)
+    {
+        int changes = 0;
+        for (int s = 0; s < int(slots_.size()); ++s)
+        {
+            const uint64_t id = slots_[s];
+            if (!id || !ex_.poll(s)) continue;
+            Job& j = jobs_[id];
+            const int rc = ex_.finish(j, s);
+            j.tDone = now;
+            if (rc)
+            {
+                j.status = FAILED;
+                j.error = ex_.error();
+                ++failed_;
+            }
+            else
+            {
+                j.status = DONE;
+                ++completed_;
+                latencies_.push_back(j.tDone - j.tSubmit);
+                workDone_ += j.work;
+                busy_ += j.tDone - j.tStart;
+            }
+            inUse_ -= j.footprint;
+            slots_[s] = 0;
+            ++changes;
+        }
+        for (auto it = queue_.begin(); it != queue_.end();)
+        {
+            Job& j = jobs_[*it];
+            if (j.queueTimeout > 0 && now - j.tSubmit > j.queueTimeout)
+            {
+                j.status = TIMEOUT;
+                j.tDone = now;
+                j.error = "queue time-out";
+                ++timedOut_;
+                it = queue_.erase(it);
+                ++changes;
+            }
+            else
+                ++it;
+        }
+        while (!queue_.empty())
+        {
+            Job& j = jobs_[queue_.front()];
+            if (inUse_ + j.footprint > budget_) break;  // head of line waits for memory
+            int s = 0;
+            while (s < int(slots_.size()) && slots_[s]) ++s;
+            if (s == int(slots_.size())) break;
+            queue_.pop_front();
+            j.tStart = now;
+            const int rc = ex_.start(j, s);
+            if (rc)
+            {
+                j.status = FAILED;
+                j.error = ex_.error();
+                j.tDone = now;
+                ++failed_;
+            }
+            else
+            {
+                j.status = RUNNING;
+                j.slot = s;
+                slots_[s] = j.id;
+                inUse_ += j.footprint;
+                peak_ = std::max(peak_, inUse_);
+                int running = 0;
+                for (uint64_t x : slots_) running += x != 0;
+                maxInFlight_ = std::max(maxInFlight_, running);
+            }
+            ++changes;
+        }
+        return changes;
+    }
+
+    bool idle() const
+    {
+        if (!queue_.empty()) return false;
+        for (uint64_t x : slots_)
+            if (x) return false;
+        return true;
+    }
+
+    const Job* get(uint64_t id) const
+    {
+        auto it = jobs_.find(id);
+        return it == jobs_.end() ? nullptr : &it->second;
+    }
+    void forget(uint64_t id) { jobs_.erase(id); }
+
+    static double percentile(std::vector<double> v, double q)
+    {
+        if (v.empty()) return 0.0;
+        std::sort(v.begin(), v.end());
+        const double pos = q * (v.size() - 1);
+        const size_t i = size_t(pos);
+        const double f = pos - i;
+        return i + 1 < v.size() ? v[i] * (1 - f) + v[i + 1] * f : v[i];
+    }
+
+    uint64_t submitted_ = 0, completed_ = 0, failed_ = 0, rejected_ = 0, cancelled_ = 0, timedOut_ = 0;
+    size_t inUse_ = 0, peak_ = 0;
+    int maxInFlight_ = 0;
+    double busy_ = 0;
+    long long workDone_ = 0;
+    std::vector<double> latencies_;
+
+private:
+    Exec& ex_;
+    std::vector<uint64_t> slots_;
+    size_t budget_;
+    uint64_t nextId_ = 0;
+    std::deque<uint64_t> queue_;
+    std::map<uint64_t, Job> jobs_;
+};
+
+}  // namespace serve
+}  // namespace cf

@@ -90,3 +90,77 @@ def superbucket_portfolio(nM=10, nK=20):
             mats.append(t)
             strikes.append(70.0 + 90.0 * i / (nK - 1))
     return mats, strikes
+
+
+# ---------------------------------------------------------------------------------------
+# Mixed serving stream: 40% Black-Scholes European values (2^14 Sobol paths), 40% Dupire
+# barrier full risk (paths log-uniform 2^16..2^20, grid 20x10 / 60x30 / 120x60, 12 / 52 /
+# 156 / 520 steps), 20% Dupire European-portfolio AADriskMulti (50-200 payoffs, 36 monthly
+# steps, 2^16 Sobol paths).  Spot 80-120, strike 0.8-1.2 x spot, barrier 1.2-1.6 x spot
+# (drawn from small sets so that models and products are stored once and reused).
+# ---------------------------------------------------------------------------------------
+SERVE_SPOTS = (80.0, 90.0, 100.0, 110.0, 120.0)
+SERVE_KR = (0.8, 0.9, 1.0, 1.1, 1.2)
+SERVE_KR_BARRIER = (0.9, 1.0, 1.1)
+SERVE_BR = (1.2, 1.4, 1.6)
+SERVE_GRIDS = ((20, 10), (60, 30), (120, 60))
+SERVE_STEPS = (12, 52, 156, 520)
+SERVE_NPAY = (50, 100, 150, 200)
+
+
+def serving_store():
+    """(models, products): id -> spec, everything the stream refers to."""
+    models, products = {}, {}
+    surf = {g: dupire_surface(*g) for g in SERVE_GRIDS}
+    for s0 in SERVE_SPOTS:
+        models[f"bs{s0:g}"] = dict(kind="bs", spot=s0, vol=0.2, rate=0.02, div=0.0, qspot=0)
+        for g in SERVE_GRIDS:
+            sp, tm, vv = surf[g]
+            for tag, mdt in (("w", 0.25), ("m", 1.0 / 12.0)):
+                models[f"dup{s0:g}_{g[0]}x{g[1]}{tag}"] = dict(kind="dupire", spot=s0, spots=sp, times=tm, vols=vv,
+                                                              maxdt=mdt)
+        for kr in SERVE_KR:
+            products[f"eu{s0:g}_{kr:g}"] = dict(kind="european", strike=kr * s0, exercise=1.0, settlement=1.0)
+        for kr in SERVE_KR_BARRIER:
+            for br in SERVE_BR:
+                for st in SERVE_STEPS:
+                    products[f"uoc{s0:g}_{kr:g}_{br:g}_{st}"] = dict(kind="uoc", strike=kr * s0, barrier=br * s0,
+                                                                      maturity=3.0, freq=3.0 / st, smooth=0.01,
+                                                                      callput=0)
+        for npay in SERVE_NPAY:
+            nk = npay // 10
+            mats, strikes = [], []
+            for j in range(10):
+                for i in range(nk):
+                    mats.append(0.3 + 0.3 * j)
+                    strikes.append(s0 * (0.8 + 0.4 * i / max(1, nk - 1)))
+            products[f"port{s0:g}_{npay}"] = dict(kind="europeans", mats=mats, strikes=strikes)
+    return models, products
+
+
+def serving_stream(n=10000, rate=2000.0, seed=2026):
+    """Seeded Poisson arrivals: list of dicts (t, kind, model, product, paths, sobol)."""
+    rs = np.random.RandomState(seed)
+    t = np.cumsum(rs.exponential(1.0 / rate, n))
+    out = []
+    for i in range(n):
+        u = rs.uniform()
+        s0 = SERVE_SPOTS[rs.randint(len(SERVE_SPOTS))]
+        if u < 0.4:
+            kr = SERVE_KR[rs.randint(len(SERVE_KR))]
+            out.append(dict(t=t[i], kind="value", model=f"bs{s0:g}", product=f"eu{s0:g}_{kr:g}", paths=1 << 14,
+                            sobol=True))
+        elif u < 0.8:
+            g = SERVE_GRIDS[rs.randint(3)]
+            st = SERVE_STEPS[rs.randint(4)]
+            kr = SERVE_KR_BARRIER[rs.randint(3)]
+            br = SERVE_BR[rs.randint(3)]
+            paths = int(round(2.0 ** rs.uniform(16, 20) / 256)) * 256
+            out.append(dict(t=t[i], kind="risk", model=f"dup{s0:g}_{g[0]}x{g[1]}w",
+                            product=f"uoc{s0:g}_{kr:g}_{br:g}_{st}", paths=paths, sobol=False))
+        else:
+            g = SERVE_GRIDS[rs.randint(3)]
+            npay = SERVE_NPAY[rs.randint(4)]
+            out.append(dict(t=t[i], kind="multi", model=f"dup{s0:g}_{g[0]}x{g[1]}m", product=f"port{s0:g}_{npay}",
+                            paths=1 << 16, sobol=True))
+    return out

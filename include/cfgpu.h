@@ -163,6 +163,58 @@ int cf_enqueue(cf_context* ctx, const char* modelId, const char* productId, cons
  * aggregate (optional), risks[nParam] (risk runs, optional). */
 int cf_fetch_result(cf_context* ctx, double* values, double* stderrs, double* aggregate, double* risks);
 
+/* ---- serving loop (no counterpart in the reference: main.h runs one call at a time on the
+ * ThreadPool, threadPool.h:30-172) -------------------------------------------------------- */
+typedef struct cf_server cf_server;
+
+/* kind 0 = value, 1 = risk of sum_k weights[k] payoff_k (weights NULL: payoff 0),
+ * 2 = AADriskMulti of a European portfolio.  queueTimeoutMs > 0 expires a request that has
+ * not started within that time. */
+typedef struct {
+    int kind;
+    const char* modelId;
+    const char* productId;
+    cf_num_param num;
+    const double* weights;
+    int nWeights;
+    double queueTimeoutMs;
+} cf_request;
+
+typedef struct {
+    uint64_t submitted, completed, failed, rejected, cancelled, timedOut;
+    double p50Ms, p99Ms, meanMs;  /* submit-to-done latency of completed requests */
+    uint64_t pathStepsDone;
+    int maxInFlight;
+    uint64_t peakFootprint;       /* bytes of admitted requests in flight at once, at most */
+} cf_serving_stats;
+
+/* Request status values of cf_server_wait. */
+#define CF_REQ_QUEUED 0
+#define CF_REQ_RUNNING 1
+#define CF_REQ_DONE 2
+#define CF_REQ_FAILED 3
+#define CF_REQ_REJECTED 4
+#define CF_REQ_CANCELLED 5
+#define CF_REQ_TIMEOUT 6
+
+/* A server with `slots` concurrent execution slots (CUDA streams) admitting requests while
+ * their device footprint fits hbmBudgetBytes. */
+int cf_server_create(cf_context* ctx, int slots, uint64_t hbmBudgetBytes, cf_server** server);
+int cf_server_destroy(cf_server* server);
+int cf_server_submit(cf_server* server, const cf_request* request, uint64_t* id);
+int cf_server_cancel(cf_server* server, uint64_t id);
+/* Blocks until the request leaves the queue / its slot (timeoutMs < 0: no limit). */
+int cf_server_wait(cf_server* server, uint64_t id, int timeoutMs, int* status);
+/* Results of a finished request: values[nPay], stderrs[nPay] (kind 0/1), *aggregate, risks
+ * (kind 1: [nParam], kind 2: [nParam*nPay]), latency from submission to completion. */
+int cf_server_result(cf_server* server, uint64_t id, double* values, double* stderrs, double* aggregate,
+                     double* risks, double* latencyMs);
+/* Forgets a finished request (frees its result storage). */
+int cf_server_release(cf_server* server, uint64_t id);
+int cf_server_stats(cf_server* server, cf_serving_stats* stats);
+/* Test hook: the next n request starts fail as if a device allocation had failed. */
+int cf_server_inject_failures(cf_server* server, int startFailures);
+
 #ifdef __cplusplus
 }
 #endif

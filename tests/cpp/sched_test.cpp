@@ -1,0 +1,173 @@
+// Host-side tests of the serving scheduler (serving_core.h) with a fake executor: admission
+// under the memory budget, arrival order, rejection, cancellation, queue time-outs, injected
+// start / finish failures, and submitters on several threads.  Prints one line per check:
+// "ok <name>" or "FAIL <name> <detail>"; exit status 0 when all pass.
+#include <cstdio>
+#include <mutex>
+#include <random>
+#include <set>
+#include <thread>
+#include <vector>
+
+#include "../../compfinance_gb300/csrc/serving_core.h"
+
+using namespace cf::serve;
+
+struct FakeExec
+{
+    double now = 0;
+    std::vector<double> doneAt = std::vector<double>(64, -1);
+    std::map<uint64_t, double> duration;
+    int failStarts = 0, failFinishes = 0;
+    std::vector<uint64_t> startOrder;
+    std::string err;
+    int start(Job& j, int s)
+    {
+        if (failStarts > 0)
+        {
+            --failStarts;
+            err = "injected allocation failure";
+            return -5;
+        }
+        startOrder.push_back(j.id);
+        doneAt[s] = now + (duration.count(j.id) ? duration[j.id] : 1.0);
+        return 0;
+    }
+    bool poll(int s) { return doneAt[s] >= 0 && now >= doneAt[s]; }
+    int finish(Job&, int s)
+    {
+        doneAt[s] = -1;
+        if (failFinishes > 0)
+        {
+            --failFinishes;
+            err = "injected result failure";
+            return -4;
+        }
+        return 0;
+    }
+    std::string error() const { return err; }
+};
+
+static int failures = 0;
+static void check(bool c, const char* name, const std::string& detail = "")
+{
+    std::printf("%s %s %s\n", c ? "ok" : "FAIL", name, detail.c_str());
+    if (!c) ++failures;
+}
+
+int main()
+{
+    {  // budget-limited admission in arrival order, slots reused
+        FakeExec ex;
+        Scheduler<FakeExec> s(ex, 4, 100);
+        std::vector<uint64_t> ids;
+        for (int i = 0; i < 10; ++i) ids.push_back(s.submit(40, 0, 0));
+        s.step(0);
+        check(ex.startOrder.size() == 2, "budget_admits_two", std::to_string(ex.startOrder.size()));
+        check(s.inUse_ <= 100, "budget_respected");
+        for (double t = 1; t <= 10; t += 1)
+        {
+            ex.now = t;
+            s.step(t);
+        }
+        check(s.completed_ == 10, "all_complete", std::to_string(s.completed_));
+        check(ex.startOrder == ids, "arrival_order");
+        check(s.peak_ <= 100 && s.maxInFlight_ == 2, "peak_footprint");
+    }
+    {  // slot-limited admission; small requests overlap
+        FakeExec ex;
+        Scheduler<FakeExec> s(ex, 3, 1000);
+        for (int i = 0; i < 7; ++i) s.submit(1, 0, 0);
+        s.step(0);
+        check(s.maxInFlight_ == 3, "slots_limit");
+    }
+    {  // rejection of a request larger than the whole budget; the queue keeps flowing
+        FakeExec ex;
+        Scheduler<FakeExec> s(ex, 2, 100);
+        const uint64_t big = s.submit(101, 0, 0);
+        const uint64_t ok = s.submit(10, 0, 0);
+        s.step(0);
+        check(s.get(big)->status == REJECTED && !s.get(big)->error.empty(), "reject_oversize");
+        check(s.get(ok)->status == RUNNING, "after_reject_runs");
+    }
+    {  // cancellation of queued requests only
+        FakeExec ex;
+        Scheduler<FakeExec> s(ex, 1, 100);
+        const uint64_t a = s.submit(10, 0, 0), b = s.submit(10, 0, 0), c = s.submit(10, 0, 0);
+        s.step(0);
+        check(!s.cancel(a, 0), "cannot_cancel_running");
+        check(s.cancel(b, 0) && s.get(b)->status == CANCELLED, "cancel_queued");
+        ex.now = 1;
+        s.step(1);
+        check(s.get(c)->status == RUNNING, "next_after_cancel");
+    }
+    {  // queue time-out
+        FakeExec ex;
+        Scheduler<FakeExec> s(ex, 1, 100);
+        ex.duration[1] = 5.0;
+        s.submit(10, 0, 0);
+        const uint64_t b = s.submit(10, 2.0, 0);
+        s.step(0);
+        ex.now = 3;
+        s.step(3);
+        check(s.get(b)->status == TIMEOUT, "queue_timeout");
+    }
+    {  // injected start and finish failures release slots and memory
+        FakeExec ex;
+        ex.failStarts = 2;
+        ex.failFinishes = 1;
+        Scheduler<FakeExec> s(ex, 2, 100);
+        for (int i = 0; i < 6; ++i) s.submit(30, 0, 0);
+        for (double t = 0; t < 10; t += 1)
+        {
+            ex.now = t;
+            s.step(t);
+        }
+        check(s.failed_ == 3 && s.completed_ == 3, "injected_failures",
+              std::to_string(s.failed_) + " " + std::to_string(s.completed_));
+        check(s.inUse_ == 0 && s.idle(), "released_after_failures");
+        check(s.get(1)->error == "injected allocation failure", "failure_message");
+    }
+    {  // random stream, several submitter threads, a scheduler thread
+        FakeExec ex;
+        Scheduler<FakeExec> s(ex, 8, 1000);
+        std::mutex mu;
+        std::set<uint64_t> all;
+        bool stop = false;
+        std::thread sched([&] {
+            double t = 0;
+            while (true)
+            {
+                std::lock_guard<std::mutex> l(mu);
+                ex.now = t;
+                s.step(t);
+                t += 0.25;
+                if (stop && s.idle()) break;
+            }
+        });
+        std::vector<std::thread> subs;
+        for (int k = 0; k < 4; ++k)
+            subs.emplace_back([&, k] {
+                std::mt19937 rng(k);
+                for (int i = 0; i < 500; ++i)
+                {
+                    std::lock_guard<std::mutex> l(mu);
+                    const uint64_t id = s.submit(1 + rng() % 300, 0, ex.now);
+                    ex.duration[id] = 0.25 * (1 + rng() % 8);
+                    all.insert(id);
+                }
+            });
+        for (auto& t : subs) t.join();
+        {
+            std::lock_guard<std::mutex> l(mu);
+            stop = true;
+        }
+        sched.join();
+        check(all.size() == 2000 && s.completed_ == 2000, "threaded_all_complete", std::to_string(s.completed_));
+        check(s.peak_ <= 1000 && s.maxInFlight_ <= 8, "threaded_limits");
+        const double p50 = Scheduler<FakeExec>::percentile(s.latencies_, 0.5),
+                     p99 = Scheduler<FakeExec>::percentile(s.latencies_, 0.99);
+        check(p50 > 0 && p99 >= p50, "percentiles");
+    }
+    return failures ? 1 : 0;
+}

@@ -121,21 +121,26 @@ def test_superbucket_finite_differences(eng):
     sb = eng.dupireSuperbucket(iv, 100.0, 1.0 / 12.0, "fdport", w, isp, mds, itm, mdt, rk, rm, nm)
     rs = np.random.RandomState(2018)
     nodes = [(rs.randint(len(rk)), rs.randint(len(rm))) for _ in range(20)]
-    h = 1e-2  # the recalibration's own rounding noise (~1e-4 of prices) swamps smaller bumps
-    worst = 0.0
+    # A single-node spread bump of a coarse risk view quickly makes the implied surface
+    # admit butterfly arbitrage (negative density -> NaN local vols), so the bump is small.
+    h = 2e-4
     scale = np.abs(sb["vega"]).max()
+    checked = 0
     for (i, j) in nodes:
         vals = []
         for sgn in (1.0, -1.0):
             sp = np.zeros((len(rk), len(rm)))
             sp[i, j] = sgn * h
             cal = eng.dupireCalib(iv, isp, mds, itm, mdt, riskView=(rk, rm, sp))
+            assert np.isfinite(cal["lVols"]).all()
             eng.putDupire(100.0, cal["spots"], cal["times"], cal["lVols"], 1.0 / 12.0, "fdmodel")
             vals.append(eng.value("fdmodel", "fdport", nm)["values"] @ w)
         fd = (vals[0] - vals[1]) / (2 * h)
-        worst = max(worst, abs(fd - sb["vega"][i, j]) / scale)
-    print("superbucket FD worst error / max vega", worst)
-    assert worst < 3e-2
+        v = sb["vega"][i, j]
+        print(f"node ({i},{j}) fd {fd:.6f} vega {v:.6f}")
+        assert abs(fd - v) <= 3e-2 * abs(v) + 2e-3 * scale, (i, j, fd, v)
+        checked += 1
+    assert checked == 20
 
 
 def test_risk_finite_differences(eng):

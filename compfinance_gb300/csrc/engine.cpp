@@ -577,11 +577,22 @@ int Context::enqueue(Slot& slot, Plan& plan, const cf_num_param& num, bool risk,
 size_t Context::footprint(const Plan& plan, const cf_num_param& num, bool risk) const
 {
     const bool sobol = num.useSobol != 0, fp32 = num.precision == CF_FP32;
-    const long long threads = std::min<long long>(sobol ? (num.numPath / 32 + 1) * 32 : (num.numPath + 1) / 2,
-                                                  (long long)numSMs * 16 * 128);
     const int NP = sobol ? 1 : 2;
+    // resident threads of the launch (the grid of enqueue), bounded by the occupancy limit
+    McParams p = plan.base;
+    p.nRisk = risk ? plan.nParam : 0;
+    p.nAcc = p.nRisk + 2 * plan.nPay + 2;
+    McLaunch l{plan.model, plan.prod, sobol ? RNG_SOBOL : RNG_MRG, fp32 ? 1 : 0, risk ? 1 : 0, 0, 0, 0};
+    size_t smem = 0;
+    mc_smem_bytes(l, p, 0, &smem);
+    int occ = 16;
+    if (mc_occupancy(l, smem, &occ) || occ < 1) occ = 16;
+    const long long needed = sobol ? (num.numPath / 32 + 1) * 32 : (num.numPath + 1) / 2;
+    const long long threads = std::min<long long>(needed, (long long)numSMs * occ * 128);
+    const int fields = plan.prod == PROD_EUROPEANS ? 1 + 3 * NP : 1 + NP + (plan.prod == PROD_UOC ? NP : 0);
     size_t b = size_t(plan.nParam + 2 * plan.nPay + 2) * 16 + size_t(plan.nPay) * 12 + 4096;
-    if (risk) b += size_t(1 + 3 * NP) * size_t(plan.nSteps + 1) * size_t(threads) * (fp32 ? 4 : 8);
+    if (risk) b += size_t(fields) * size_t(plan.nSteps + 1) * size_t(threads) * (fp32 ? 4 : 8);
+    if (plan.prod == PROD_EUROPEANS && risk) b += size_t(plan.nPay + plan.nEv) * size_t(plan.nParam) * 16;
     return b;
 }
 

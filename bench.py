@@ -101,22 +101,31 @@ class Clocks:
         return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": mx, "reasons": reasons, "samples": len(rows)}
 
 
-def cpu_baseline(seconds=12.0, threads=None):
-    """The oracle's hand-written adjoint (multi-threaded) on a bounded sample of the workload."""
+def _cpu_case():
     import oracle as O
     s, t, v = W.dupire_surface(*GRID)
     u = W.UOC_BARRIER
     m = O.Model(dict(kind="dupire", spot=W.DUPIRE_SPOT, spots=s, times=t, vols=v, maxdt=W.DUPIRE_MAXDT))
     p = O.Product(dict(kind="uoc", strike=u["strike"], barrier=u["barrier"], maturity=u["maturity"],
                        freq=u["monitor_freq"], smooth=u["smooth"], callput=0))
-    threads = threads or os.cpu_count() or 1
-    w = np.array([1.0, 0.0])
+    return O, m, p, np.array([1.0, 0.0])
+
+
+def _cpu_sample_size(O, m, p, w, threads, seconds):
+    """Paths (even) that the threaded CPU adjoint runs in about `seconds`."""
     n = 1 << 12
     t0 = time.perf_counter()
     O.risk(m, p, 0, n, w, fast=True, threads=threads)
     dt = time.perf_counter() - t0
     n = int(min(1 << 23, max(n, n * seconds / max(dt, 1e-3))))
-    n -= n % 2
+    return n - n % 2
+
+
+def cpu_baseline(seconds=12.0, threads=None):
+    """The oracle's hand-written adjoint (multi-threaded) on a bounded sample of the workload."""
+    O, m, p, w = _cpu_case()
+    threads = threads or os.cpu_count() or 1
+    n = _cpu_sample_size(O, m, p, w, threads, seconds)
     t0 = time.perf_counter()
     O.risk(m, p, 0, n, w, fast=True, threads=threads)
     dt = time.perf_counter() - t0
@@ -150,14 +159,31 @@ def serving_leg(eng, n, seed):
 
 
 def run_reference(args):
+    """The reference arm: the CPU restatement of the reference's path (the reference's own
+    sources are not on the GPU host) on all host threads, W untimed + K timed steps, each step
+    a bounded sample of the workload (~4 s)."""
     rank, world, _ = env_rank()
     if rank != 0:
         return 0
-    cb = cpu_baseline()
-    out = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "paths/s", "n_gpus": args.gpus,
-           "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "dtype": "f64",
+    O, m, p, w = _cpu_case()
+    threads = os.cpu_count() or 1
+    n = _cpu_sample_size(O, m, p, w, threads, 4.0)
+    for _ in range(args.warmup):
+        O.risk(m, p, 0, min(n, 1 << 14), w, fast=True, threads=threads)
+    ts = []
+    for k in range(args.steps):
+        t0 = time.perf_counter()
+        O.risk(m, p, 0, n, w, fast=True, threads=threads, seed1=W.MRG_SEEDS[0] + k)
+        ts.append(time.perf_counter() - t0)
+    tot = sum(ts)
+    value = n * args.steps / tot
+    cb = {"value": value, "unit": "paths/s", "cores": threads, "kind": "port",
+          "sample": f"{n} paths per step of the same workload (FP64, hand-written adjoint, {threads} threads)"}
+    out = {"impl": "reference", "metric": METRIC, "value": value, "unit": "paths/s", "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": tot / args.steps * 1e3,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
            "data": "synthetic", "config": CONFIG, "cpu_baseline": cb,
-           "e2e": {"value": cb["value"], "unit": "paths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+           "e2e": {"value": value, "unit": "paths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
     return 0
 
@@ -171,6 +197,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-stream leg")
     ap.add_argument("--serve-requests", type=int, default=10000)
+    ap.add_argument("--paths", type=int, default=NPATH,
+                    help="paths per step (default 2^22; smaller cases are for profiler captures only)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -179,6 +207,10 @@ def main():
     import torch
     from compfinance_gb300 import Engine, NumericalParam
 
+    npath = args.paths
+    config = dict(CONFIG, paths=npath)
+    if npath != NPATH:
+        config["workload"] = CONFIG["workload"].replace("2^22paths", f"{npath}paths")
     rank, world, local = env_rank()
     if world > 1:
         import torch.distributed as dist
@@ -195,8 +227,8 @@ def main():
     npay, npar, dim = eng.shapes("dupire", "uoc")
     # Each rank simulates its own 2^22 paths (independent seeds): weak scaling, no exchange.
     seed1 = W.MRG_SEEDS[0] + 7919 * rank
-    num32 = NumericalParam(numPath=NPATH, precision="fp32", seed1=seed1)
-    num64 = NumericalParam(numPath=NPATH, precision="fp64", seed1=seed1)
+    num32 = NumericalParam(numPath=npath, precision="fp32", seed1=seed1)
+    num64 = NumericalParam(numPath=npath, precision="fp64", seed1=seed1)
     flush = torch.empty(64 << 20, dtype=torch.float32, device="cuda")
 
     def timed(num, steps, warmup):
@@ -236,7 +268,7 @@ def main():
     # equal-error check: FP32 vs FP64 on the same paths, in Monte Carlo standard errors
     se = []
     for k in range(8):
-        eng.enqueue("dupire", "uoc", NumericalParam(numPath=NPATH // 4, precision="fp32", seed1=1000 + k, seed2=77 + k),
+        eng.enqueue("dupire", "uoc", NumericalParam(numPath=npath // 4, precision="fp32", seed1=1000 + k, seed2=77 + k),
                     risk=True)
         se.append(eng.fetch(npay, npar)[3])
     se = np.std(np.array(se), axis=0, ddof=1) / 2.0  # std at N/4 -> standard error at N
@@ -255,9 +287,9 @@ def main():
     e2e_t = (time.perf_counter() - w0) / ke
     h1, d1 = eng.transfer_stats()
 
-    steps_tot = NPATH * dim
+    steps_tot = npath * dim
     per_step = t32 / args.steps
-    value = world * NPATH / per_step
+    value = world * npath / per_step
     pk = peaks()
     sm_max = float(pk.get("sm_max_mhz", 2070.0))
     peak_fp32 = 152 * 128 * 2 * sm_max * 1e6 / 1e12
@@ -274,9 +306,9 @@ def main():
     out = {
         "metric": METRIC, "value": value, "unit": "paths/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": per_step * 1e3, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": CONFIG,
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config,
         "path_steps_per_s": value * dim,
-        "fp64": {"value": world * NPATH / (t64 / steps64), "unit": "paths/s", "ms_per_step": t64 / steps64 * 1e3,
+        "fp64": {"value": world * npath / (t64 / steps64), "unit": "paths/s", "ms_per_step": t64 / steps64 * 1e3,
                  "steps": steps64},
         "fp32_over_fp64": (t64 / steps64) / per_step,
         "equal_error": {"price_fp32_minus_fp64_in_stderr": price_err_se,
@@ -287,7 +319,7 @@ def main():
                      "peak_source": "152 SM x 128 FP32 lanes x 2 x sm_max_mhz of MEASURED_PEAKS.json "
                                     "(no tensor-core or HBM bound applies)",
                      "flops_per_path_step": FLOPS_PER_PATH_STEP},
-        "e2e": {"value": world * NPATH / e2e_t, "unit": "paths/s", "h2d_bytes_per_step": (h1 - h0) // ke,
+        "e2e": {"value": world * npath / e2e_t, "unit": "paths/s", "h2d_bytes_per_step": (h1 - h0) // ke,
                 "d2h_bytes_per_step": (d1 - d0) // ke},
         "gpu_launches": launches,
         "clocks": clocks,

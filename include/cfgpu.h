@@ -144,6 +144,19 @@ int cf_dupire_superbucket(cf_context* ctx, const cf_ivs* ivs, double spot, doubl
                           int nStrikes, const double* mats, int nMats, const cf_num_param* num, int refSeeding,
                           double* value, double* delta, double* vega, double* microbucket);
 
+/* AADriskAggregate without any device allocation.  No counterpart in the reference.
+ * For callers that cannot let a library allocate device memory during a call (memory
+ * already reserved by another allocator, or a cudaMalloc / cudaFree stall is unacceptable):
+ * the same risk kernel as cf_aad_risk_aggregate, with all its device storage in one 64 MiB
+ * static device array held by every GPU that loads the library until process exit.  The
+ * (model, product) pair must already be lowered (e.g. by cf_shapes); the first call on a
+ * device looks up the array's address and should come before any stream capture; calls
+ * that overlap on the GPU share the array and race; requests whose scratch does not fit
+ * are rejected with CF_E_SHAPE.  Results: payoffValues[nPay], *aggregateValue, risks[nParam]. */
+int cf_aad_risk_aggregate_noalloc(cf_context* ctx, const char* modelId, const char* productId,
+                                  const double* notionals, const cf_num_param* num, double* payoffValues,
+                                  double* aggregateValue, double* risks);
+
 /* ---- RNG access (sobol.h, mrg32k3a.h), for bit-exactness checks -------------------- */
 /* Sobol integer points of paths [firstPath, firstPath+nPaths), dimension dim: out[nPaths*dim]. */
 int cf_sobol_points(cf_context* ctx, int dim, int64_t firstPath, int nPaths, uint32_t* out);

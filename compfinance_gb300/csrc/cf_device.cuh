@@ -64,36 +64,12 @@ __device__ __forceinline__ void fix_add(long long* slot, Real v)
     if (lo) atomicAdd(reinterpret_cast<unsigned long long*>(slot + 1), (unsigned long long)lo);
 }
 
-// Single-word accumulation of FP32 adjoint contributions, in units of 2^-32, integer
-// operations only.  Contributions with |v| >= 2^12 (rare: paths near a smoothed barrier)
-// go to the global two-word accumulator gslot instead, so a slab word only ever receives
-// values below 2^44 units and, flushed every NODE_FLUSH_UNITS, cannot overflow.
-constexpr int FIX1_SHIFT = 32;
-template <class Real>
-__device__ __forceinline__ void fix_add(long long* slot, Real v);
-__device__ __forceinline__ void fix1_add(long long* slot, float v, long long* gslot)
-{
-    const unsigned b = __float_as_uint(v);
-    const int E = int((b >> 23) & 0xffu);
-    if (E < 94) return;  // |v| < 2^-33: below half a unit
-    if (E > 138)
-    {
-        fix_add(gslot, v);
-        return;
-    }
-    const unsigned m = (b & 0x7fffffu) | 0x800000u;
-    const int s = E - 118;  // v 2^32 = m 2^s, s in [-24, 20]
-    long long n = s >= 0 ? (long long)m << s : (long long)((m + (1u << (-s - 1))) >> (-s));
-    if (b >> 31) n = -n;
-    atomicAdd(reinterpret_cast<unsigned long long*>(slot), (unsigned long long)n);
-}
-
-// Flush of a single-word slab entry into a global hi/lo pair.
-__device__ __forceinline__ void fix1_flush(long long* g, long long n)
+// A node slab word in units of 2^-NODE_SHIFT, added exactly into a global hi/lo pair.
+__device__ __forceinline__ void node_flush(long long* g, long long n)
 {
     if (!n) return;
-    const long long hi = n >> (FIX1_SHIFT - FIX_HI_SHIFT);
-    const long long lo = (n - (hi << (FIX1_SHIFT - FIX_HI_SHIFT))) << (FIX_LO_SHIFT - FIX1_SHIFT);
+    const long long hi = n >> (NODE_SHIFT - FIX_HI_SHIFT);
+    const long long lo = (n - (hi << (NODE_SHIFT - FIX_HI_SHIFT))) << (FIX_LO_SHIFT - NODE_SHIFT);
     if (hi) atomicAdd(reinterpret_cast<unsigned long long*>(g), (unsigned long long)hi);
     if (lo) atomicAdd(reinterpret_cast<unsigned long long*>(g + 1), (unsigned long long)lo);
 }

@@ -22,6 +22,20 @@ constexpr int FIX_HI_SHIFT = 20;
 constexpr int FIX_LO_SHIFT = 60;
 constexpr int FIX_CARRY_SHIFT = FIX_LO_SHIFT - FIX_HI_SHIFT;
 
+// FP32 local-vol adjoints (risk launches of the Dupire model) are gathered in two stages.
+// Each warp adds, per simulation step, the adjoints of the step's vol row Y[i][.] into a
+// per-warp row of int32 words in units of 2^-ROW_SHIFT (one native shared-memory add per
+// contribution; |contribution| < ROW_MAX, so a word that receives at most 64 of them per
+// step cannot overflow; larger ones go straight to the global accumulators).  After the
+// step the warp multiplies each row word by the step's integer time weights
+// W = round(w 2^WEIGHT_SHIFT) and adds the exact int64 product to the block's node slab, in
+// units of 2^-NODE_SHIFT.  Every operation is an exact integer operation on per-contribution
+// roundings, so the sums do not depend on how paths are grouped into warps or blocks.
+constexpr int ROW_SHIFT = 16;
+constexpr float ROW_MAX = 256.0f;
+constexpr int WEIGHT_SHIFT = 23;
+constexpr int NODE_SHIFT = ROW_SHIFT + WEIGHT_SHIFT;
+
 // Accumulator layout (one hi/lo pair each):
 //   [0, nRisk)                   parameter adjoints (risk mode; 0 in value mode)
 //   [nRisk, nRisk+nPay)          sum of payoff k
@@ -64,6 +78,10 @@ struct McParams
     const float* cAf;
     const double* cBd;    // [nSteps] d Y[i][j] / d vol[j][colB] (0 when flat)
     const float* cBf;
+    const int* wAi;       // [nSteps] round(cA 2^WEIGHT_SHIFT), FP32 form's node weights
+    const int* wBi;
+    int nodeFlushUnits;   // FP32 risk: units per thread between node slab flushes (>= 1)
+    int nodeDirect;       // FP32 risk: 1 = add row products straight to the global accumulators
     int stageY;           // 1: stage Y into shared memory (cp.async.bulk)
     // Bucket index of the log-spot grid: bucket b of nBuckets equal slices of [X0, X_last]
     // holds the upper_bound of its left edge, a starting guess for the interpolation search.

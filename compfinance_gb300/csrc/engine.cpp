@@ -4,6 +4,8 @@
 // (allocate/init/timeline/defline/payoffLabels/parameterLabels), main.h entry points.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -234,7 +236,7 @@ int Context::buildPlan(const ModelDesc& m, const ProductDesc& pd, Plan& plan)
     std::vector<double> ev(7 * size_t(plan.nEv), 0.0);
     double frontSpot = m.spot;
     size_t oBs = 0, oX = 0, oInv = 0, oY = 0, oXf = 0, oInvf = 0, oYf = 0, oCA = 0, oCB = 0, oCAf = 0, oCBf = 0,
-           oColA = 0, oColB = 0, oBsF = 0, oBucket = 0;
+           oColA = 0, oColB = 0, oBsF = 0, oBucket = 0, oWA = 0, oWB = 0;
 
     if (m.kind == MODEL_BS)
     {
@@ -346,6 +348,22 @@ int Context::buildPlan(const ModelDesc& m, const ProductDesc& pd, Plan& plan)
         oCB = pk.vec(cBv);
         oCAf = pk.vec(to_f(cAv));
         oCBf = pk.vec(to_f(cBv));
+        // FP32 risk: integer time weights of the row-to-node gather, and the node slab's
+        // flush interval: a slab word receives at most 4 warps x (steps touching its time
+        // column) products below 2^50 per unit, and must stay below 2^63.
+        std::vector<int> wA(n), wB(n), touch(nT, 0);
+        for (int i = 0; i < n; ++i)
+        {
+            wA[i] = int(std::llround(std::ldexp(cAv[i], WEIGHT_SHIFT)));
+            wB[i] = int(std::llround(std::ldexp(cBv[i], WEIGHT_SHIFT)));
+            ++touch[colA[i]];
+            if (colB[i] != colA[i]) ++touch[colB[i]];
+        }
+        const int sMax = *std::max_element(touch.begin(), touch.end());
+        P.nodeFlushUnits = std::max(1, std::min(4, 2048 / std::max(1, sMax)));
+        P.nodeDirect = sMax >= 2048 ? 1 : 0;
+        oWA = pk.vec(wA);
+        oWB = pk.vec(wB);
         plan.nSteps = n;
         plan.yBytesD = Y.size() * 8;
         plan.yBytesF = Y.size() * 4;
@@ -402,6 +420,8 @@ int Context::buildPlan(const ModelDesc& m, const ProductDesc& pd, Plan& plan)
         P.cBd = (const double*)D(oCB);
         P.cAf = (const float*)D(oCAf);
         P.cBf = (const float*)D(oCBf);
+        P.wAi = (const int*)D(oWA);
+        P.wBi = (const int*)D(oWB);
     }
     P.evAtStep = (const int*)D(oEv);
     P.evD = (const double*)D(oEvD);

@@ -10,7 +10,10 @@
 //             from maturity back to today, replacing the reference's tape
 //             (mcBase.h:427-532 records ~5 nodes per step and sweeps them back).
 // Node adjoints of the local-vol grid, parameter adjoints and payoff sums are added to a
-// block-private shared-memory slab in exact fixed point, flushed once per block.
+// block-private shared-memory slab in exact fixed point, flushed once per block.  In the
+// FP32 form the local-vol adjoints first go through a per-warp row of the current step (see
+// ROW_SHIFT in cf_params.h): two native 32-bit shared adds per path-step instead of four
+// 64-bit ones, and one exact weighted add per touched grid spot per warp and step.
 #pragma once
 #include <type_traits>
 
@@ -19,9 +22,6 @@
 namespace cf {
 
 constexpr int MC_BLOCK = 128;
-// FP32 risk runs flush their single-word node slab after this many units per thread
-// (<= 1024 paths per block between flushes), so no word can overflow.
-constexpr int NODE_FLUSH_UNITS = 4;
 
 template <class R>
 __device__ __forceinline__ const R* pick(const double* d, const float* f);
@@ -35,7 +35,7 @@ __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(
 // Shared-memory carve-up; identical on host (sizing) and device (pointers).
 struct SmemLayout
 {
-    size_t slab, node, mbar, X, inv, bucket, Y, base, total;
+    size_t slab, node, rows, mbar, X, inv, bucket, Y, base, total;
 };
 
 __host__ __device__ inline SmemLayout mc_layout(int model, int rng, int fp32, int stageY, const McParams& p,
@@ -50,6 +50,9 @@ __host__ __device__ inline SmemLayout mc_layout(int model, int rng, int fp32, in
     // local-vol node adjoints: one word each in the FP32 form, two in the FP64 form
     L.node = off;
     if (model == MODEL_DUPIRE && p.nRisk > 0) off += align16(size_t(p.nS) * p.nT * (fp32 ? 8 : 16));
+    // FP32 form: one int32 row of the current step's vol adjoints per warp
+    L.rows = off;
+    if (model == MODEL_DUPIRE && p.nRisk > 0 && fp32) off += align16(size_t(block / 32) * p.nS * 4);
     L.mbar = off;
     off += 16;
     L.X = L.inv = L.bucket = L.Y = L.base = off;
@@ -75,6 +78,9 @@ __global__ void __launch_bounds__(MC_BLOCK) mc_kernel(const McParams p)
 {
     constexpr int NP = RNGK == RNG_MRG ? 2 : 1;
     constexpr bool F32 = std::is_same<Real, float>::value;
+    // FP32 local-vol adjoints gathered through per-warp step rows (the warp's step loops then
+    // stay converged: lanes without a unit run them with no paths)
+    constexpr bool ROWACC = F32 && MODEL == MODEL_DUPIRE && RISK;
     extern __shared__ __align__(128) unsigned char smem[];
 
     const SmemLayout L = mc_layout(MODEL, RNGK, F32, p.stageY, p, MC_BLOCK);
@@ -82,11 +88,14 @@ __global__ void __launch_bounds__(MC_BLOCK) mc_kernel(const McParams p)
     long long* paySlab = slab + 8;
     long long* node = reinterpret_cast<long long*>(smem + L.node);
     const int tid = threadIdx.x;
+    const int lane = tid & 31;
     const int nNodes = (MODEL == MODEL_DUPIRE && RISK) ? p.nS * p.nT : 0;
     const int nodeWords = nNodes * (F32 ? 1 : 2);
+    int* rows = reinterpret_cast<int*>(smem + L.rows) + (tid >> 5) * p.nS;  // this warp's row
     for (int i = tid; i < 2 * (4 + 2 * p.nPay + 2); i += MC_BLOCK) slab[i] = 0;
     for (int i = tid; i < nodeWords; i += MC_BLOCK) node[i] = 0;
-    int overflow = 0;
+    if (ROWACC)
+        for (int i = tid; i < (MC_BLOCK / 32) * p.nS; i += MC_BLOCK) reinterpret_cast<int*>(smem + L.rows)[i] = 0;
 
     const int nSteps = p.nSteps;
     const int nS = p.nS, nT = p.nT;
@@ -180,8 +189,47 @@ __global__ void __launch_bounds__(MC_BLOCK) mc_kernel(const McParams p)
         }
     };
 
+    // FP32 local-vol adjoints.  rowAdd: contribution c to spot j of step s's vol row, into the
+    // warp's row (or, when |c| >= ROW_MAX, exactly into the global accumulators of the two
+    // nodes the row interpolates).  nodeAdd: an exact int64 product, in units of
+    // 2^-NODE_SHIFT, into the block's node slab (or global when it could overflow the slab).
+    // rowFlush: after step s, the warp moves its row into the nodes (time weights W of s).
+    auto rowAdd = [&](int s, int j, float c) {
+        if (c == 0.0f) return;
+        if (fabsf(c) < ROW_MAX)
+            atomicAdd(&rows[j], __float2int_rn(c * float(1 << ROW_SHIFT)));
+        else
+        {
+            fix_add(&p.acc[2 * (1 + j * nT + p.colA[s])], c * p.cAf[s]);
+            if (p.cBf[s] != 0.0f) fix_add(&p.acc[2 * (1 + j * nT + p.colB[s])], c * p.cBf[s]);
+        }
+    };
+    auto nodeAdd = [&](int idx, long long v) {
+        constexpr long long LIM = 1LL << 50;
+        if (!p.nodeDirect && v < LIM && v > -LIM)
+            atomicAdd(reinterpret_cast<unsigned long long*>(&node[idx]), (unsigned long long)v);
+        else
+            node_flush(&p.acc[2 * (1 + idx)], v);
+    };
+    auto rowFlush = [&](int s) {
+        __syncwarp();
+        const long long WA = p.wAi[s], WB = p.wBi[s];
+        const int ca = p.colA[s], cb = p.colB[s];
+        for (int j = lane; j < nS; j += 32)
+        {
+            const int r = rows[j];
+            if (r != 0)
+            {
+                rows[j] = 0;
+                nodeAdd(j * nT + ca, WA * r);
+                if (WB != 0) nodeAdd(j * nT + cb, WB * r);
+            }
+        }
+        __syncwarp();
+    };
+
     // ---------------------------------------------------------------------------------
-    // One work unit: nAct (1 or 2) paths driven by the Gaussian generator gen(i).
+    // One work unit: nAct (0, 1 or 2) paths driven by the Gaussian generator gen(i).
     // ---------------------------------------------------------------------------------
     auto runUnit = [&](int nAct, auto&& gen) {
         Real x[NP], alive[NP], euro[NP], fE[NP], dE[NP], nE[NP], agg[NP];
@@ -263,7 +311,7 @@ __global__ void __launch_bounds__(MC_BLOCK) mc_kernel(const McParams p)
         }
         for (int i = 0; i < nSteps; ++i)
         {
-            const Real g = gen(i);
+            const Real g = nAct ? gen(i) : Real(0);
             if (RISK) SCR(F_G, i) = g;
 #pragma unroll
             for (int a = 0; a < NP; ++a)
@@ -442,27 +490,26 @@ __global__ void __launch_bounds__(MC_BLOCK) mc_kernel(const McParams p)
                     const Real q = ga - v;             // d x_{s+1} / d v
                     const Real av = ax[a] * q;
                     ax[a] += av * slope;               // d x_{s+1} / d x_s = 1 + q dv/dx
-                    const int ca = p.colA[s], cb = p.colB[s];
-                    const Real wa = cA[s], wb = cB[s];
-                    auto put = [&](int j, Real aY) {
-                        if (aY == Real(0)) return;
-                        if (F32)
-                        {
-                            fix1_add(&node[j * nT + ca], float(aY * wa), &p.acc[2 * (1 + j * nT + ca)]);
-                            if (wb != Real(0))
-                                fix1_add(&node[j * nT + cb], float(aY * wb), &p.acc[2 * (1 + j * nT + cb)]);
-                        }
-                        else
-                        {
-                            fix_add(&node[2 * (j * nT + ca)], aY * wa);
-                            if (wb != Real(0)) fix_add(&node[2 * (j * nT + cb)], aY * wb);
-                        }
-                    };
-                    if (flat) put(k, av);
+                    if (ROWACC)
+                    {
+                        rowAdd(s, k, flat ? av : av * (Real(1) - t));
+                        if (!flat) rowAdd(s, k + 1, av * t);
+                    }
                     else
                     {
-                        put(k, av * (Real(1) - t));
-                        put(k + 1, av * t);
+                        const int ca = p.colA[s], cb = p.colB[s];
+                        const Real wa = cA[s], wb = cB[s];
+                        auto put = [&](int j, Real aY) {
+                            if (aY == Real(0)) return;
+                            fix_add(&node[2 * (j * nT + ca)], aY * wa);
+                            if (wb != Real(0)) fix_add(&node[2 * (j * nT + cb)], aY * wb);
+                        };
+                        if (flat) put(k, av);
+                        else
+                        {
+                            put(k, av * (Real(1) - t));
+                            put(k + 1, av * t);
+                        }
                     }
                 }
                 else
@@ -475,6 +522,7 @@ __global__ void __launch_bounds__(MC_BLOCK) mc_kernel(const McParams p)
                     ax[a] *= E;
                 }
             }
+            if (ROWACC) rowFlush(s);
         }
         if (MODEL == MODEL_DUPIRE)
         {
@@ -503,12 +551,12 @@ __global__ void __launch_bounds__(MC_BLOCK) mc_kernel(const McParams p)
         }
     };
 
-    // Single-word node words flushed to the global hi/lo accumulators (block-wide).
+    // FP32 node slab flushed to the global hi/lo accumulators (block-wide).
     auto flushNodes = [&]() {
         __syncthreads();
         for (int i = tid; i < nNodes; i += MC_BLOCK)
         {
-            fix1_flush(&p.acc[2 * (1 + i)], node[i]);
+            node_flush(&p.acc[2 * (1 + i)], node[i]);
             node[i] = 0;
         }
         __syncthreads();
@@ -526,12 +574,9 @@ __global__ void __launch_bounds__(MC_BLOCK) mc_kernel(const McParams p)
         for (long long it = 0; it < per; ++it)
         {
             const long long u = u0 + it;
-            if (u < u1)
-            {
-                const int nAct = (2 * u + 1 < p.nPath) ? 2 : 1;
-                runUnit(nAct, [&](int) { return mrg_gauss<Real>(mrg_next(st)); });
-            }
-            if (F32 && nNodes && (it + 1) % NODE_FLUSH_UNITS == 0) flushNodes();
+            const int nAct = u < u1 ? ((2 * u + 1 < p.nPath) ? 2 : 1) : 0;
+            if (ROWACC || nAct) runUnit(nAct, [&](int) { return mrg_gauss<Real>(mrg_next(st)); });
+            if (ROWACC && (it + 1) % p.nodeFlushUnits == 0) flushNodes();
         }
     }
     else
@@ -539,7 +584,7 @@ __global__ void __launch_bounds__(MC_BLOCK) mc_kernel(const McParams p)
         // Sobol: warp w of the grid takes batches b = w, w + W, ...; lane l runs index
         // n = 32b + l (path n-1).  state(n) = state(32b) ^ state(l) (gray code is linear
         // over the disjoint bit ranges of 32b and l).
-        const int lane = tid & 31, wib = tid >> 5;
+        const int wib = tid >> 5;
         const int pitch = nSteps | 1;
         unsigned* base = reinterpret_cast<unsigned*>(smem + L.base) + wib * pitch;
         const long long W = T / 32, gw = tg / 32;
@@ -548,15 +593,16 @@ __global__ void __launch_bounds__(MC_BLOCK) mc_kernel(const McParams p)
         for (long long it = 0; it < rounds; ++it)
         {
             const long long b = gw + it * W;
-            if (F32 && nNodes && it > 0 && it % NODE_FLUSH_UNITS == 0) flushNodes();
+            if (ROWACC && it > 0 && it % p.nodeFlushUnits == 0) flushNodes();
             if (b >= nBatches) continue;
             __syncwarp();
             for (int d = lane; d < nSteps; d += 32)
                 base[d] = sobol_state(p.sobolDir, nSteps, d, (unsigned long long)b * 32);
             __syncwarp();
             const long long n = b * 32 + lane;
-            if (n >= 1 && n <= p.nPath)
-                runUnit(1, [&](int i) {
+            const int nAct = (n >= 1 && n <= p.nPath) ? 1 : 0;
+            if (ROWACC || nAct)
+                runUnit(nAct, [&](int i) {
                     return sobol_gauss<Real>(base[i] ^ sobol_state(p.sobolDir, nSteps, i, (unsigned long long)lane));
                 });
         }
@@ -570,12 +616,11 @@ __global__ void __launch_bounds__(MC_BLOCK) mc_kernel(const McParams p)
         for (int i = tid; i < nScal; i += MC_BLOCK) fix_flush(&p.acc[2 * i], &slab[2 * i]);
         for (int i = tid; i < nNodes; i += MC_BLOCK)
         {
-            if (F32) fix1_flush(&p.acc[2 * (1 + i)], node[i]);
+            if (F32) node_flush(&p.acc[2 * (1 + i)], node[i]);
             else fix_flush(&p.acc[2 * (1 + i)], &node[2 * i]);
         }
     }
     for (int i = tid; i < 2 * nPay + 2; i += MC_BLOCK) fix_flush(&p.acc[2 * (p.nRisk + i)], &paySlab[2 * i]);
-    if (overflow) atomicOr(p.err, DEVERR_FIXED_RANGE);
 }
 
 }  // namespace cf

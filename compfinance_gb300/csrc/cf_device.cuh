@@ -236,8 +236,8 @@ __device__ __forceinline__ float mrg_gauss_f(unsigned d)
 {
     const unsigned half = 2147483544u;              // (m1 + 1) / 2
     const bool sup = d > half;
-    const unsigned up = sup ? 4294967088u - d : d;  // exact integer 1 - p scaled
-    return inv_normal_up((float)up * (1.0f / 4294967088.0f), sup);
+    const unsigned up = sup ? 4294967088u - d : d;  // exact integer 1 - p scaled, below 2^31
+    return inv_normal_up(__int2float_rn(int(up)) * (1.0f / 4294967088.0f), sup);
 }
 
 // Gaussian of a Sobol integer state s (sobol.h:110-116, truncated constant sobol.h:26).
@@ -248,8 +248,12 @@ __device__ __forceinline__ double sobol_gauss_d(unsigned s)
 __device__ __forceinline__ float sobol_gauss_f(unsigned s)
 {
     const bool sup = s >= 2147483648u;
-    const unsigned up = sup ? (unsigned)(4294967296ULL - s) : s;
-    return inv_normal_up((float)up * 2.3283064365386963e-10f, sup);
+    // up in [1, 2^31].  2^31 (s = 2^31, the coordinate 1/2 of every dimension at the first
+    // point) does not fit a signed int; a plain cast of it was compiled to a signed conversion
+    // and turned 1/2 into -1/2 (a NaN Gaussian).  2^31 - 1 rounds to the same float 2^31, so
+    // the signed conversion of up - [up == 2^31] is exact for every up.
+    const unsigned up = sup ? 0u - s : s;
+    return inv_normal_up(__int2float_rn(int(up - (up >> 31))) * 2.3283064365386963e-10f, sup);
 }
 
 template <class Real>

@@ -116,6 +116,19 @@ struct McParams
     void* scratch;
     long long scratchThreads;
     int scratchFields;
+
+    // FP32 Dupire risk kernel (dupire_risk32): interval tables of the log-spot grid.
+    // Interval lo in [0, nS] is the upper_bound of the state among the knots; for each step
+    // and interval the local vol is y + d t with t = (x - xr) ir in [0, 1), flat (d = ir = 0)
+    // outside the grid.
+    int fast32;           // 1 when the plan carries these tables (the launch may use the kernel)
+    const float* xsF;     // [nS + 2] knots with -inf / +inf sentinels at both ends
+    const float* irF;     // [nS + 1][2] (xr, ir) per interval
+    const float* tdF;     // [nSteps][nS + 1][2] (y, d) per step and interval
+    const int* bucketF;   // [nBucketsF] upper_bound of each bucket's left edge; buckets are
+                          // narrower than 2/3 of the smallest knot spacing (at most one knot each)
+    int nBucketsF;
+    float bX0F, bInvWF;
 };
 
 // Kernel configuration chosen by the host.
@@ -124,11 +137,16 @@ struct McLaunch
     int model, prod, rng, fp32, risk;
     int grid, block;
     size_t smem;
+    int fast;             // 1: FP32 Dupire risk through dupire_risk32
 };
 
 int launch_mc(const McLaunch& l, const McParams& p, void* stream);   // returns cudaError_t
 int mc_smem_bytes(const McLaunch& l, const McParams& p, int stageY, size_t* bytes);
 int mc_occupancy(const McLaunch& l, size_t smem, int* blocksPerSM);
+int mc_scratch_fields(const McLaunch& l);   // reverse-sweep scratch fields of a risk launch
+// Whether a (model, product, precision, mode) launch of this plan runs dupire_risk32
+// (CF_FAST32=0 in the environment selects the generic kernel instead).
+int mc_use_fast32(const McParams& plan, int prod, int fp32, int risk);
 int launch_finalize(const McParams& p, double invN, double* out, void* stream);
 
 }  // namespace cf

@@ -236,7 +236,7 @@ int Context::buildPlan(const ModelDesc& m, const ProductDesc& pd, Plan& plan)
     std::vector<double> ev(7 * size_t(plan.nEv), 0.0);
     double frontSpot = m.spot;
     size_t oBs = 0, oX = 0, oInv = 0, oY = 0, oXf = 0, oInvf = 0, oYf = 0, oCA = 0, oCB = 0, oCAf = 0, oCBf = 0,
-           oColA = 0, oColB = 0, oBsF = 0, oBucket = 0, oWA = 0, oWB = 0;
+           oColA = 0, oColB = 0, oBsF = 0, oBucket = 0, oWA = 0, oWB = 0, oXs = 0, oIr = 0, oTd = 0, oBf = 0;
 
     if (m.kind == MODEL_BS)
     {
@@ -364,6 +364,58 @@ int Context::buildPlan(const ModelDesc& m, const ProductDesc& pd, Plan& plan)
         P.nodeDirect = sMax >= 2048 ? 1 : 0;
         oWA = pk.vec(wA);
         oWB = pk.vec(wB);
+        // FP32 risk kernel (dupire_risk32): knots with sentinels, (xr, ir) per interval,
+        // (y, d) per step and interval, and buckets narrower than 2/3 of the smallest knot
+        // spacing.  Products whose dates are not monitoring dates plus a final maturity, grids
+        // with more than 510 spots or with knots too close for 4096 buckets use the generic kernel.
+        {
+            std::vector<float> xs(size_t(nS) + 2), irv(2 * size_t(nS + 1), 0.0f), tdv(2 * size_t(n) * (nS + 1));
+            xs[0] = -INFINITY;
+            xs[nS + 1] = INFINITY;
+            for (int j = 0; j < nS; ++j) xs[j + 1] = Xf[j];
+            for (int lo = 1; lo < nS; ++lo)
+            {
+                irv[2 * lo] = Xf[lo - 1];
+                irv[2 * lo + 1] = float(inv[lo - 1]);
+            }
+            for (int i = 0; i < n; ++i)
+            {
+                const double* y = &Y[size_t(i) * nS];
+                float* o = &tdv[2 * size_t(i) * (nS + 1)];
+                o[0] = float(y[0]);
+                for (int lo = 1; lo < nS; ++lo)
+                {
+                    o[2 * lo] = float(y[lo - 1]);
+                    o[2 * lo + 1] = float(y[lo] - y[lo - 1]);
+                }
+                o[2 * nS] = float(y[nS - 1]);
+            }
+            double minGap = INFINITY;
+            for (int j = 0; j + 1 < nS; ++j) minGap = std::min(minGap, double(Xf[j + 1]) - double(Xf[j]));
+            const double range = nS > 1 ? double(Xf[nS - 1]) - double(Xf[0]) : 0.0;
+            int nBf = 8;
+            while (nBf < 4096 && range / nBf > minGap / 1.5) nBf *= 2;
+            const double wf = range > 0 ? range / nBf : 1.0;
+            std::vector<int> bf(nBf);
+            for (int b = 0; b < nBf; ++b)
+            {
+                const double edge = double(Xf[0]) + b * wf;
+                bf[b] = int(std::upper_bound(Xf.begin(), Xf.end(), edge,
+                                             [](double e, float x) { return e < double(x); }) - Xf.begin());
+            }
+            bool evOk = evAtStep[n] == plan.nEv - 1;
+            if (pd.kind == PROD_EUROPEAN)
+                for (int i = 0; i < n; ++i) evOk = evOk && evAtStep[i] < 0;
+            P.fast32 = (pd.kind == PROD_UOC || pd.kind == PROD_EUROPEAN) && evOk && nS <= 510 && minGap > 0 &&
+                       range / nBf <= minGap / 1.5;
+            P.nBucketsF = nBf;
+            P.bX0F = Xf[0];
+            P.bInvWF = float(1.0 / wf);
+            oXs = pk.vec(xs);
+            oIr = pk.vec(irv);
+            oTd = pk.vec(tdv);
+            oBf = pk.vec(bf);
+        }
         plan.nSteps = n;
         plan.yBytesD = Y.size() * 8;
         plan.yBytesF = Y.size() * 4;
@@ -422,6 +474,10 @@ int Context::buildPlan(const ModelDesc& m, const ProductDesc& pd, Plan& plan)
         P.cBf = (const float*)D(oCBf);
         P.wAi = (const int*)D(oWA);
         P.wBi = (const int*)D(oWB);
+        P.xsF = (const float*)D(oXs);
+        P.irF = (const float*)D(oIr);
+        P.tdF = (const float*)D(oTd);
+        P.bucketF = (const int*)D(oBf);
     }
     P.evAtStep = (const int*)D(oEv);
     P.evD = (const double*)D(oEvD);
@@ -530,16 +586,27 @@ int Context::enqueue(Slot& slot, Plan& plan, const cf_num_param& num, bool risk,
     p.err = reinterpret_cast<int*>(wbase + wBytes + accBytes);
     CF_CUDA(cudaMemsetAsync(p.acc, 0, accBytes + 16, st));
 
-    McLaunch l{plan.model, plan.prod, sobol ? RNG_SOBOL : RNG_MRG, fp32 ? 1 : 0, risk ? 1 : 0, 0, 0, 0};
-    // Shared-memory staging of the interpolated local vols (a bulk copy through the TMA
-    // unit): used only when it costs no occupancy; otherwise the table is read through L1.
+    McLaunch l{plan.model, plan.prod, sobol ? RNG_SOBOL : RNG_MRG, fp32 ? 1 : 0, risk ? 1 : 0, 0, 0, 0, 0};
+    // FP32 Dupire risk runs dupire_risk32 when the plan has its tables and its node slab fits
+    // an SM; everything else runs the generic mc_kernel.
     int stage = 0;
     size_t smem0 = 0, smem1 = 0;
-    mc_smem_bytes(l, p, 0, &smem0);
     int occ0 = 0, occ1 = 0;
-    rc = mc_occupancy(l, smem0, &occ0);
-    if (rc) return cuda_fail(cudaError_t(rc), "occupancy");
-    if (plan.model == MODEL_DUPIRE)
+    l.fast = mc_use_fast32(plan.base, plan.prod, l.fp32, l.risk);
+    if (l.fast)
+    {
+        mc_smem_bytes(l, p, 0, &smem0);
+        if (smem0 > 200 * 1024 || mc_occupancy(l, smem0, &occ0) || occ0 < 1) l.fast = 0;
+    }
+    if (!l.fast)
+    {
+        mc_smem_bytes(l, p, 0, &smem0);
+        rc = mc_occupancy(l, smem0, &occ0);
+        if (rc) return cuda_fail(cudaError_t(rc), "occupancy");
+    }
+    // Shared-memory staging of the interpolated local vols (a bulk copy through the TMA
+    // unit): used only when it costs no occupancy; otherwise the table is read through L1.
+    if (plan.model == MODEL_DUPIRE && !l.fast)
     {
         mc_smem_bytes(l, p, 1, &smem1);
         const char* env = std::getenv("CF_STAGE_Y");
@@ -565,8 +632,7 @@ int Context::enqueue(Slot& slot, Plan& plan, const cf_num_param& num, bool risk,
     l.block = 128;
     if (risk)
     {
-        const int NP = sobol ? 1 : 2;
-        p.scratchFields = 1 + NP + (plan.prod == PROD_UOC ? NP : 0);
+        p.scratchFields = mc_scratch_fields(l);
         // kernels index the scratch with 32-bit offsets: keep fields*(steps+1)*threads < 2^31
         const long long perThread = (long long)p.scratchFields * (plan.nSteps + 1);
         const long long maxThreads = ((1LL << 31) - 1) / perThread;
@@ -602,14 +668,15 @@ size_t Context::footprint(const Plan& plan, const cf_num_param& num, bool risk) 
     McParams p = plan.base;
     p.nRisk = risk ? plan.nParam : 0;
     p.nAcc = p.nRisk + 2 * plan.nPay + 2;
-    McLaunch l{plan.model, plan.prod, sobol ? RNG_SOBOL : RNG_MRG, fp32 ? 1 : 0, risk ? 1 : 0, 0, 0, 0};
+    McLaunch l{plan.model, plan.prod, sobol ? RNG_SOBOL : RNG_MRG, fp32 ? 1 : 0, risk ? 1 : 0, 0, 0, 0, 0};
+    l.fast = mc_use_fast32(plan.base, plan.prod, l.fp32, l.risk);
     size_t smem = 0;
     mc_smem_bytes(l, p, 0, &smem);
     int occ = 16;
     if (mc_occupancy(l, smem, &occ) || occ < 1) occ = 16;
     const long long needed = sobol ? (num.numPath / 32 + 1) * 32 : (num.numPath + 1) / 2;
     const long long threads = std::min<long long>(needed, (long long)numSMs * occ * 128);
-    const int fields = plan.prod == PROD_EUROPEANS ? 1 + 3 * NP : 1 + NP + (plan.prod == PROD_UOC ? NP : 0);
+    const int fields = plan.prod == PROD_EUROPEANS ? 1 + 3 * NP : mc_scratch_fields(l);
     size_t b = size_t(plan.nParam + 2 * plan.nPay + 2) * 16 + size_t(plan.nPay) * 12 + 4096;
     if (risk) b += size_t(fields) * size_t(plan.nSteps + 1) * size_t(threads) * (fp32 ? 4 : 8);
     if (plan.prod == PROD_EUROPEANS && risk) b += size_t(plan.nPay + plan.nEv) * size_t(plan.nParam) * 16;

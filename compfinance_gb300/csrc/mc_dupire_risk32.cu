@@ -1,0 +1,495 @@
+// FP32 Dupire risk kernel: value and path-wise adjoint of one aggregate of the European or
+// smoothed up-and-out payoffs (mcSimulAAD, mcBase.h:427-532, for Dupire, mcMdlDupire.h:238-280,
+// with the products of mcPrd.h:113-288), FP32 path arithmetic, exact fixed-point sums.
+//
+// A block of 128 threads runs work units (an antithetic mrg32k3a pair, or one Sobol path per
+// thread) in three phases:
+//  1. forward: each thread simulates its unit and stores per step one packed word per path
+//     (the interval of the log-spot grid, the interpolation weight t to 22 bits, and whether
+//     the monitoring date at that point fell in the barrier's smoothing band) plus the
+//     unit's Gaussian; band dates also store the survival factor before the date and the
+//     spot.  The forward itself uses the quantised weight, so the reverse sweep replays
+//     exactly the operations of the forward.
+//  2. compaction: paths whose adjoint seed is zero (knocked out, or out of the money at
+//     maturity) contribute nothing to any risk; the block lists the others.
+//  3. reverse: the listed paths, one per thread, are swept back from maturity to today in
+//     lock step (one __syncthreads per step).  Local-vol adjoints of step s go into per-warp
+//     rows of int32 words (units of 2^-ROW_SHIFT, one native shared add per contribution);
+//     after the step, thread j moves spot j of the four rows into the node slab, which it
+//     alone owns, scaled by the step's integer time weights: plain loads and stores, no
+//     64-bit atomics.  Each contribution is rounded once, so every sum is independent of how
+//     paths are grouped into warps, blocks and launches.
+#include <cuda_runtime.h>
+
+#include "cf_device.cuh"
+
+namespace cf {
+
+namespace {
+
+constexpr int RB = 128;                 // threads per block
+constexpr int RW = RB / 32;             // warps per block
+constexpr int T_BITS = 22;              // interpolation weight bits of the packed step word
+constexpr unsigned T_MASK = (1u << T_BITS) - 1;
+constexpr unsigned BAND_BIT = 1u << T_BITS;
+constexpr int LO_SHIFT = T_BITS + 1;    // interval index in bits 23..31
+// t in [0, 1) is quantised through the float t + 2 in [2, 3), whose low 22 mantissa bits
+// are round(t 2^22): no conversion instruction either way
+constexpr unsigned TWO_BITS = 0x40000000u;         // bits of 2.0f
+constexpr float T_MAX = 1.0f - 1.0f / 4194304.0f;  // t + 2 stays below 3
+// A row word receives at most 32 contributions per step (one path per lane), each below
+// ROW_MAX32 * 2^ROW_SHIFT = 2^25 in magnitude: the word stays below 2^30.
+constexpr float ROW_MAX32 = 512.0f;
+constexpr int KSTEP = 1;                // reverse steps per block barrier (rows per group)
+constexpr long long SLAB_LIMIT = 1LL << 61;  // node slab words move to global beyond this
+
+__host__ __device__ inline size_t a16(size_t x) { return (x + 15) & ~size_t(15); }
+
+struct R32Layout
+{
+    size_t slab, node, rows, xs, ir, bucket, listIdx, listAx, listAl, cnt, base, total;
+    int rowPitch;
+};
+
+__host__ __device__ inline R32Layout r32_layout(int rng, const McParams& p)
+{
+    R32Layout L;
+    size_t off = 0;
+    L.slab = off;
+    off += a16(size_t(4 + 2 * p.nPay + 2) * 16);
+    L.node = off;
+    off += a16(size_t(p.nS) * p.nT * 8);
+    L.rowPitch = (p.nS + 2) & ~1;  // nS + 1 words (the last interval's right node), even
+    L.rows = off;
+    off += a16(size_t(2 * KSTEP) * RW * L.rowPitch * 4);
+    L.xs = off;
+    off += a16(size_t(p.nS + 2) * 4);
+    L.ir = off;
+    off += a16(size_t(p.nS + 1) * 8);
+    L.bucket = off;
+    off += a16(size_t(p.nBucketsF) * 4);
+    L.listIdx = off;
+    off += a16(size_t(2 * RB) * 4);
+    L.listAx = off;
+    off += a16(size_t(2 * RB) * 4);
+    L.listAl = off;
+    off += a16(size_t(2 * RB) * 4);
+    L.cnt = off;
+    off += 16;
+    L.base = off;
+    if (rng == RNG_SOBOL) off += a16(size_t(RW) * (size_t(p.nSteps) | 1) * 4);
+    L.total = off;
+    return L;
+}
+
+template <int PROD, int RNGK>
+__global__ void __launch_bounds__(RB, 8) dupire_risk32(const McParams p)
+{
+    constexpr int NP = RNGK == RNG_MRG ? 2 : 1;
+    constexpr bool UOC = PROD == PROD_UOC;
+    extern __shared__ __align__(128) unsigned char smem[];
+    const R32Layout L = r32_layout(RNGK, p);
+    long long* slab = reinterpret_cast<long long*>(smem + L.slab);  // [0,2) spot adjoint, payoffs from 8
+    long long* paySlab = slab + 8;
+    long long* node = reinterpret_cast<long long*>(smem + L.node);
+    int* rows = reinterpret_cast<int*>(smem + L.rows);              // [2 KSTEP][RW][rowPitch]
+    float* sXs = reinterpret_cast<float*>(smem + L.xs);
+    float2* sIr = reinterpret_cast<float2*>(smem + L.ir);
+    int* sBucket = reinterpret_cast<int*>(smem + L.bucket);
+    int* listIdx = reinterpret_cast<int*>(smem + L.listIdx);
+    float* listAx = reinterpret_cast<float*>(smem + L.listAx);
+    float* listAl = reinterpret_cast<float*>(smem + L.listAl);
+    int* cnt = reinterpret_cast<int*>(smem + L.cnt);
+
+    const int tid = threadIdx.x, lane = tid & 31, wib = tid >> 5;
+    const int nS = p.nS, nT = p.nT, nSteps = p.nSteps, nPay = p.nPay;
+    const int rowPitch = L.rowPitch;
+    for (int i = tid; i < 2 * (4 + 2 * nPay + 2); i += RB) slab[i] = 0;
+    for (int i = tid; i < nS * nT; i += RB) node[i] = 0;
+    for (int i = tid; i < 2 * KSTEP * RW * rowPitch; i += RB) rows[i] = 0;
+    for (int i = tid; i < nS + 2; i += RB) sXs[i] = p.xsF[i];
+    for (int i = tid; i < nS + 1; i += RB) sIr[i] = make_float2(p.irF[2 * i], p.irF[2 * i + 1]);
+    for (int i = tid; i < p.nBucketsF; i += RB) sBucket[i] = p.bucketF[i];
+    __syncthreads();
+
+    const float2* td = reinterpret_cast<const float2*>(p.tdF);
+    const int tPitch = nS + 1;
+    const float strike = (float)p.strike, barSmooth = (float)p.barSmooth, minusSmooth = (float)p.minusSmooth,
+                twoSmooth = (float)p.twoSmooth;
+    const float invTwo = -1.0f / twoSmooth;
+    const float logBand = p.logBandF;
+    const float s0 = p.s0f;
+    const float spot = (float)p.spot;
+    const float w0 = nPay > 0 ? p.wf[0] : 0.0f, w1 = nPay > 1 ? p.wf[1] : 0.0f;
+    const float bX0 = p.bX0F, bInvW = p.bInvWF;
+    const int nB = p.nBucketsF;
+
+    // scratch [field][point][thread], 32-bit offsets (the host keeps it below 2^31 elements)
+    const int Ti = int(gridDim.x) * RB;
+    const int rowStride = (nSteps + 1) * Ti;
+    float* scr = reinterpret_cast<float*>(p.scratch);
+    constexpr int F_G = 0, F_W = 1, F_B = 1 + NP, F_S = 1 + 2 * NP;
+    const int myCol = int(blockIdx.x) * RB + tid;
+
+    // upper_bound of xs among the knots (exact: a bucket holds at most one knot, and the
+    // bucket of xs computed in FP32 is off by at most one)
+    auto search = [&](float xs) -> int {
+        const float fb = (xs - bX0) * bInvW;
+        int b = 0;
+        if (fb > 0.0f) b = fb < float(nB - 1) ? int(fb) : nB - 1;
+        const int l0 = sBucket[b];
+        const int lo = l0 + (sXs[l0 + 1] <= xs ? 1 : 0) - (sXs[l0] > xs ? 1 : 0);
+        return lo < nS ? lo : nS;  // +inf would pass the last sentinel
+    };
+
+    // ---------------------------------------------------------------------------------
+    // One unit: forward, payoff sums, adjoint seeds.  Returns the seeds in ax/aAl and
+    // whether each path is live (nonzero seed).
+    // ---------------------------------------------------------------------------------
+    float axOut[NP], alOut[NP];
+    bool live[NP];
+    auto forward = [&](int nAct, auto&& gen) {
+        float x[NP], alive[NP], euro[NP], sT[NP], bLast[NP];
+        bool dead[NP];
+        unsigned flag[NP];
+#pragma unroll
+        for (int a = 0; a < NP; ++a)
+        {
+            x[a] = 0.0f;
+            alive[a] = 1.0f;
+            euro[a] = sT[a] = bLast[a] = 0.0f;
+            dead[a] = false;
+            flag[a] = 0;
+            live[a] = false;
+            axOut[a] = alOut[a] = 0.0f;
+        }
+        if (!nAct) return;
+
+        // product date at point i (i < nSteps: monitoring only; i == nSteps: maturity)
+        auto event = [&](int i, int a) {
+            const bool last = i == nSteps;
+            if (!UOC)
+            {
+                if (last)
+                {
+                    const float S = s0 * expf(x[a]);
+                    sT[a] = S;
+                    euro[a] = S - strike > 0.0f ? S - strike : 0.0f;
+                }
+                return;
+            }
+            if (!last && (dead[a] || !(x[a] > logBand))) return;
+            const float S = s0 * expf(x[a]);
+            if (!dead[a])
+            {
+                if (S > barSmooth) dead[a] = true;
+                else if (S > minusSmooth)
+                {
+                    if (last) bLast[a] = alive[a];
+                    else
+                    {
+                        scr[(F_B + a) * rowStride + i * Ti + myCol] = alive[a];
+                        scr[(F_S + a) * rowStride + i * Ti + myCol] = S;
+                    }
+                    alive[a] *= (barSmooth - S) / twoSmooth;
+                    flag[a] = 1;
+                }
+            }
+            if (last)
+            {
+                sT[a] = S;
+                const float m = p.callPut ? (strike - S) : (S - strike);
+                euro[a] = m > 0.0f ? m : 0.0f;
+            }
+        };
+
+        if (p.evAtStep[0] >= 0)
+#pragma unroll
+            for (int a = 0; a < NP; ++a)
+                if (a < nAct) event(0, a);
+        for (int s = 0; s < nSteps; ++s)
+        {
+            const float g = gen(s);
+            scr[F_G * rowStride + s * Ti + myCol] = g;
+            const float2* trow = td + size_t(s) * tPitch;
+#pragma unroll
+            for (int a = 0; a < NP; ++a)
+            {
+                if (a >= nAct) break;
+                const float ga = a ? -g : g;
+                const int lo = search(x[a]);
+                const float2 ir = sIr[lo];
+                const float t2 = fminf((x[a] - ir.x) * ir.y, T_MAX) + 2.0f;
+                const unsigned tq = __float_as_uint(t2) & T_MASK;
+                const float2 yd = __ldg(trow + lo);
+                const float v = fmaf(yd.y, t2 - 2.0f, yd.x);
+                reinterpret_cast<unsigned*>(scr)[(F_W + a) * rowStride + s * Ti + myCol] =
+                    (unsigned(lo) << LO_SHIFT) | (flag[a] ? BAND_BIT : 0u) | tq;
+                flag[a] = 0;  // the flag of point s + 1 is set by its date, if any
+                x[a] += v * (-0.5f * v + ga);
+            }
+            if (__ldg(p.evAtStep + s + 1) >= 0)
+#pragma unroll
+                for (int a = 0; a < NP; ++a)
+                    if (a < nAct) event(s + 1, a);
+        }
+
+        // payoffs, sums, adjoint seeds
+#pragma unroll
+        for (int a = 0; a < NP; ++a)
+        {
+            if (a >= nAct) break;
+            float ax, aAl = 0.0f, agg;
+            if (UOC)
+            {
+                const float p0 = dead[a] ? 0.0f : alive[a] * euro[a];
+                fix_add(&paySlab[0], p0);
+                fix_add(&paySlab[2 * nPay], p0 * p0);
+                fix_add(&paySlab[2], euro[a]);
+                fix_add(&paySlab[2 * (nPay + 1)], euro[a] * euro[a]);
+                agg = w0 * p0 + w1 * euro[a];
+                const float aEuro = dead[a] ? w1 : w0 * alive[a] + w1;
+                aAl = dead[a] ? 0.0f : w0 * euro[a];
+                const float m = p.callPut ? (strike - sT[a]) : (sT[a] - strike);
+                float aF = m > 0.0f ? (p.callPut ? -aEuro : aEuro) : 0.0f;
+                if (flag[a])
+                {
+                    aF += aAl * bLast[a] * invTwo;
+                    aAl *= (barSmooth - sT[a]) / twoSmooth;
+                }
+                ax = aF * sT[a];
+            }
+            else
+            {
+                fix_add(&paySlab[0], euro[a]);
+                fix_add(&paySlab[2 * nPay], euro[a] * euro[a]);
+                agg = w0 * euro[a];
+                ax = euro[a] > 0.0f ? w0 * sT[a] : 0.0f;
+            }
+            fix_add(&paySlab[2 * (2 * nPay)], agg);
+            fix_add(&paySlab[2 * (2 * nPay + 1)], agg * agg);
+            axOut[a] = ax;
+            alOut[a] = aAl;
+            live[a] = ax != 0.0f || aAl != 0.0f;
+        }
+    };
+
+    // contribution c (units of 1) to spot j of step s's vol row: exact global fixed point when
+    // too large for a row word
+    auto bigAdd = [&](int s, int j, float c) {
+        fix_add(&p.acc[2 * (1 + j * nT + __ldg(p.colA + s))], c * __ldg(p.cAf + s));
+        const float cb = __ldg(p.cBf + s);
+        if (cb != 0.0f) fix_add(&p.acc[2 * (1 + j * nT + __ldg(p.colB + s))], c * cb);
+    };
+    // thread-owned node slab word += v (units of 2^-NODE_SHIFT)
+    auto nodeAdd = [&](int idx, long long v) {
+        long long n = node[idx] + v;
+        if (n > SLAB_LIMIT || n < -SLAB_LIMIT)
+        {
+            node_flush(&p.acc[2 * (1 + idx)], n);
+            n = 0;
+        }
+        node[idx] = n;
+    };
+
+    // ---------------------------------------------------------------------------------
+    // Compaction and reverse sweep of one unit round (block-uniform).
+    // ---------------------------------------------------------------------------------
+    auto reverse = [&]() {
+        const unsigned b0 = __ballot_sync(0xffffffffu, live[0]);
+        const unsigned b1 = NP == 2 ? __ballot_sync(0xffffffffu, live[NP - 1]) : 0u;
+        if (lane == 0) cnt[wib] = __popc(b0) + __popc(b1);
+        __syncthreads();
+        int total = 0, off = 0;
+#pragma unroll
+        for (int w = 0; w < RW; ++w)
+        {
+            const int c = cnt[w];
+            off += w < wib ? c : 0;
+            total += c;
+        }
+        const unsigned lt = (1u << lane) - 1u;
+        if (live[0])
+        {
+            const int pos = off + __popc(b0 & lt);
+            listIdx[pos] = tid * 2;
+            listAx[pos] = axOut[0];
+            listAl[pos] = alOut[0];
+        }
+        if (NP == 2 && live[NP - 1])
+        {
+            const int pos = off + __popc(b0) + __popc(b1 & lt);
+            listIdx[pos] = tid * 2 + 1;
+            listAx[pos] = axOut[NP - 1];
+            listAl[pos] = alOut[NP - 1];
+        }
+        __syncthreads();
+        const int nPass = (total + RB - 1) / RB;
+        for (int pass = 0; pass < nPass; ++pass)
+        {
+            const int idx = pass * RB + tid;
+            const bool has = idx < total;
+            int a = 0, col = 0;
+            float ax = 0.0f, aAl = 0.0f;
+            if (has)
+            {
+                const int e = listIdx[idx];
+                a = e & 1;
+                col = int(blockIdx.x) * RB + (e >> 1);
+                ax = listAx[idx];
+                aAl = listAl[idx];
+            }
+            const unsigned* sw = reinterpret_cast<const unsigned*>(scr) + (F_W + a) * rowStride + col;
+            const float* sg = scr + F_G * rowStride + col;
+            int* myRow = rows + wib * rowPitch;
+            unsigned wNext = 0;  // packed word of the step after s: band flag of point s + 1
+            // steps nSteps-1 .. 0 in groups of KSTEP; group g uses row sets (g & 1) KSTEP + k
+            for (int s0 = nSteps - 1, g = 0; s0 >= 0; s0 -= KSTEP, ++g)
+            {
+                const int kEnd = s0 + 1 < KSTEP ? s0 + 1 : KSTEP;
+                const int set0 = (g & 1) * KSTEP;
+                for (int k = 0; k < kEnd; ++k)
+                {
+                    const int s = s0 - k;
+                    if (!has) continue;
+                    if (UOC && (wNext & BAND_BIT))
+                    {
+                        const int i = s + 1;
+                        const float before = scr[(F_B + a) * rowStride + i * Ti + col];
+                        const float S = scr[(F_S + a) * rowStride + i * Ti + col];
+                        const float aF = aAl * before * invTwo;
+                        aAl *= (barSmooth - S) / twoSmooth;
+                        ax += aF * S;
+                    }
+                    const unsigned W = sw[s * Ti];
+                    const float g1 = sg[s * Ti];
+                    const float ga = a ? -g1 : g1;
+                    const int lo = int(W >> LO_SHIFT);
+                    const float t = __uint_as_float(TWO_BITS | (W & T_MASK)) - 2.0f;
+                    const float2 yd = __ldg(td + size_t(s) * tPitch + lo);
+                    const float2 ir = sIr[lo];
+                    const float v = fmaf(yd.y, t, yd.x);
+                    const float av = ax * (ga - v);      // d x_{s+1} / d v = g - v
+                    ax += av * (yd.y * ir.y);            // d x_{s+1} / d x_s = 1 + (g - v) dv/dx
+                    if (av != 0.0f)
+                    {
+                        const int jl = lo - (lo > 0 ? 1 : 0);
+                        const bool inner = lo > 0 && lo < nS;  // two nodes; one at flat ends
+                        const float cR = av * t, cL = av - cR;
+                        if (fabsf(av) < ROW_MAX32)
+                        {
+                            int* row = myRow + (set0 + k) * RW * rowPitch;
+                            atomicAdd(&row[jl], __float2int_rn(cL * 65536.0f));
+                            if (inner && cR != 0.0f) atomicAdd(&row[jl + 1], __float2int_rn(cR * 65536.0f));
+                        }
+                        else
+                        {
+                            bigAdd(s, jl, cL);
+                            if (inner && cR != 0.0f) bigAdd(s, jl + 1, cR);
+                        }
+                    }
+                    wNext = W;
+                }
+                __syncthreads();
+                // the group's rows -> node slab; spot j = 4 q + w belongs to thread (w, q mod 32)
+                for (int k = 0; k < kEnd; ++k)
+                {
+                    const int s = s0 - k;
+                    const long long WA = __ldg(p.wAi + s), WB = __ldg(p.wBi + s);
+                    const int ca = __ldg(p.colA + s), cb = __ldg(p.colB + s);
+                    int* rs = rows + (set0 + k) * RW * rowPitch;
+                    for (int j = 4 * lane + wib; j < nS; j += 4 * 32)
+                    {
+                        int* r = rs + j;
+                        const int r0 = r[0], r1 = r[rowPitch], r2 = r[2 * rowPitch], r3 = r[3 * rowPitch];
+                        if (r0 | r1 | r2 | r3)
+                        {
+                            r[0] = r[rowPitch] = r[2 * rowPitch] = r[3 * rowPitch] = 0;
+                            const long long sum = (long long)r0 + r1 + r2 + r3;
+                            nodeAdd(j * nT + ca, WA * sum);
+                            if (WB != 0) nodeAdd(j * nT + cb, WB * sum);
+                        }
+                    }
+                }
+            }
+            if (has)
+            {
+                if (UOC && (wNext & BAND_BIT))  // band at today's date
+                {
+                    const float before = scr[(F_B + a) * rowStride + col];
+                    const float S = scr[(F_S + a) * rowStride + col];
+                    ax += aAl * before * invTwo * S;
+                }
+                fix_add(&slab[0], ax / spot);  // x_0 = log(spot)
+            }
+            __syncthreads();
+        }
+    };
+
+    const long long T = (long long)gridDim.x * RB;
+    const long long tg = (long long)blockIdx.x * RB + tid;
+    if (RNGK == RNG_MRG)
+    {
+        const long long nUnits = (p.nPath + 1) / 2;
+        const long long per = (nUnits + T - 1) / T;
+        const long long u0 = tg * per;
+        const long long u1 = u0 + per < nUnits ? u0 + per : nUnits;
+        MrgState st{};
+        if (u0 < u1) st = mrg_jump(p.seed1, p.seed2, (unsigned long long)u0 * nSteps, p.mrgJumpA, p.mrgJumpB);
+        for (long long it = 0; it < per; ++it)  // the same trip count for every thread of the grid
+        {
+            const long long u = u0 + it;
+            const int nAct = u < u1 ? ((2 * u + 1 < p.nPath) ? 2 : 1) : 0;
+            forward(nAct, [&](int) { return mrg_gauss<float>(mrg_next(st)); });
+            reverse();
+        }
+    }
+    else
+    {
+        // Sobol: warp w takes batches b = w, w + W, ...; lane l runs index n = 32b + l
+        // (path n-1); state(n) = state(32b) ^ state(l).
+        const int pitch = nSteps | 1;
+        unsigned* base = reinterpret_cast<unsigned*>(smem + L.base) + wib * pitch;
+        const long long W = T / 32, gw = tg / 32;
+        const long long nBatches = p.nPath / 32 + 1;
+        const long long rounds = (nBatches + W - 1) / W;
+        for (long long it = 0; it < rounds; ++it)
+        {
+            const long long b = gw + it * W;
+            int nAct = 0;
+            if (b < nBatches)
+            {
+                __syncwarp();
+                for (int d = lane; d < nSteps; d += 32)
+                    base[d] = sobol_state(p.sobolDir, nSteps, d, (unsigned long long)b * 32);
+                __syncwarp();
+                const long long n = b * 32 + lane;
+                nAct = (n >= 1 && n <= p.nPath) ? 1 : 0;
+            }
+            forward(nAct, [&](int i) {
+                return sobol_gauss<float>(base[i] ^ sobol_state(p.sobolDir, nSteps, i, (unsigned long long)lane));
+            });
+            reverse();
+        }
+    }
+
+    __syncthreads();
+    if (tid == 0) fix_flush(&p.acc[0], &slab[0]);
+    for (int i = tid; i < nS * nT; i += RB) node_flush(&p.acc[2 * (1 + i)], node[i]);
+    for (int i = tid; i < 2 * nPay + 2; i += RB) fix_flush(&p.acc[2 * (p.nRisk + i)], &paySlab[2 * i]);
+}
+
+}  // namespace
+
+const void* dupire_risk32_ptr(int prod, int rng)
+{
+    if (prod == PROD_UOC && rng == RNG_MRG) return (const void*)&dupire_risk32<PROD_UOC, RNG_MRG>;
+    if (prod == PROD_UOC && rng == RNG_SOBOL) return (const void*)&dupire_risk32<PROD_UOC, RNG_SOBOL>;
+    if (prod == PROD_EUROPEAN && rng == RNG_MRG) return (const void*)&dupire_risk32<PROD_EUROPEAN, RNG_MRG>;
+    if (prod == PROD_EUROPEAN && rng == RNG_SOBOL) return (const void*)&dupire_risk32<PROD_EUROPEAN, RNG_SOBOL>;
+    return nullptr;
+}
+
+size_t dupire_risk32_smem(int rng, const McParams& p) { return r32_layout(rng, p).total; }
+
+}  // namespace cf

@@ -2,6 +2,8 @@
 // the launch itself (cudaLaunchKernel on the caller's stream).
 #include <cuda_runtime.h>
 
+#include <cstdlib>
+
 #include "mc_kernel.cuh"
 
 namespace cf {
@@ -10,9 +12,12 @@ const void* mc_kernel_ptr_bs_f64(int prod, int rng, int risk);
 const void* mc_kernel_ptr_bs_f32(int prod, int rng, int risk);
 const void* mc_kernel_ptr_dupire_f64(int prod, int rng, int risk);
 const void* mc_kernel_ptr_dupire_f32(int prod, int rng, int risk);
+const void* dupire_risk32_ptr(int prod, int rng);
+size_t dupire_risk32_smem(int rng, const McParams& p);
 
 static const void* kernel_ptr(const McLaunch& l)
 {
+    if (l.fast) return dupire_risk32_ptr(l.prod, l.rng);
     if (l.model == MODEL_BS)
         return l.fp32 ? mc_kernel_ptr_bs_f32(l.prod, l.rng, l.risk) : mc_kernel_ptr_bs_f64(l.prod, l.rng, l.risk);
     return l.fp32 ? mc_kernel_ptr_dupire_f32(l.prod, l.rng, l.risk)
@@ -21,8 +26,25 @@ static const void* kernel_ptr(const McLaunch& l)
 
 int mc_smem_bytes(const McLaunch& l, const McParams& p, int stageY, size_t* bytes)
 {
-    *bytes = mc_layout(l.model, l.rng, l.fp32, stageY, p, MC_BLOCK).total;
+    *bytes = l.fast ? dupire_risk32_smem(l.rng, p) : mc_layout(l.model, l.rng, l.fp32, stageY, p, MC_BLOCK).total;
     return 0;
+}
+
+int mc_scratch_fields(const McLaunch& l)
+{
+    const int NP = l.rng == RNG_SOBOL ? 1 : 2;
+    // dupire_risk32: Gaussian, packed step word per path, and for the barrier the survival
+    // factor and spot of band dates per path; generic kernel: Gaussian, state per path, and
+    // for the barrier the survival factor of band dates per path
+    if (l.fast) return 1 + NP + (l.prod == PROD_UOC ? 2 * NP : 0);
+    return 1 + NP + (l.prod == PROD_UOC ? NP : 0);
+}
+
+int mc_use_fast32(const McParams& plan, int prod, int fp32, int risk)
+{
+    if (!plan.fast32 || !fp32 || !risk || (prod != PROD_UOC && prod != PROD_EUROPEAN)) return 0;
+    const char* env = std::getenv("CF_FAST32");
+    return env && env[0] == '0' ? 0 : 1;
 }
 
 int mc_occupancy(const McLaunch& l, size_t smem, int* blocksPerSM)

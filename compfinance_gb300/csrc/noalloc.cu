@@ -138,14 +138,23 @@ extern "C" int cf_aad_risk_aggregate_noalloc(cf_context* ctx, const char* modelI
     const size_t offScr = offOut + outBytes;
     if (offScr >= CF_NOALLOC_BYTES) return fail_c(CF_E_SHAPE, "noalloc: accumulators exceed the 64 MiB arena");
 
-    McLaunch l{plan->model, plan->prod, sobol ? RNG_SOBOL : RNG_MRG, fp32 ? 1 : 0, 1, 0, 128, 0};
+    McLaunch l{plan->model, plan->prod, sobol ? RNG_SOBOL : RNG_MRG, fp32 ? 1 : 0, 1, 0, 128, 0, 0};
     size_t smem = 0;
     p.stageY = 0;
-    mc_smem_bytes(l, p, 0, &smem);
     int occ = 0;
-    if ((rc = mc_occupancy(l, smem, &occ)) || occ < 1) return fail_c(CF_E_SHAPE, "noalloc: kernel does not fit");
-    const int NP = sobol ? 1 : 2;
-    p.scratchFields = 1 + NP + (plan->prod == PROD_UOC ? NP : 0);
+    // the kernel choice of the allocating entry point (cf_aad_risk_aggregate)
+    l.fast = mc_use_fast32(p, plan->prod, l.fp32, 1);
+    if (l.fast)
+    {
+        mc_smem_bytes(l, p, 0, &smem);
+        if (smem > 200 * 1024 || mc_occupancy(l, smem, &occ) || occ < 1) l.fast = 0;
+    }
+    if (!l.fast)
+    {
+        mc_smem_bytes(l, p, 0, &smem);
+        if ((rc = mc_occupancy(l, smem, &occ)) || occ < 1) return fail_c(CF_E_SHAPE, "noalloc: kernel does not fit");
+    }
+    p.scratchFields = mc_scratch_fields(l);
     const size_t perThread = size_t(p.scratchFields) * size_t(plan->nSteps + 1) * (fp32 ? 4 : 8);
     const long long fitBlocks = (long long)((CF_NOALLOC_BYTES - offScr) / (perThread * 128));
     if (fitBlocks < 1) return fail_c(CF_E_SHAPE, "noalloc: one block of reverse-sweep scratch exceeds the arena");

@@ -166,3 +166,67 @@ def test_fp32_form_within_tenth_of_stderr(eng, grid):
         assert np.all(np.abs(r32["risks"] - r64["risks"])[mask] <= 0.1 * se[mask])
         # nodes with no measurable variance must agree to FP32 rounding
         assert np.all(np.abs(r32["risks"] - r64["risks"])[~mask] <= 1e-6 * np.abs(r64["risks"]).max())
+
+
+def _se_fp64(eng, mid, pid, n):
+    """Standard error of each risk at n paths, from 8 independent mrg32k3a seed pairs at n/4."""
+    rs = np.array([eng.AADriskOne(mid, pid, num(0, n // 4, "fp64", 1000 + k, 77 + k))["risks"] for k in range(8)])
+    return rs.std(axis=0, ddof=1) / 2.0
+
+
+@pytest.mark.parametrize("prod", ["uoc", "european"])
+@pytest.mark.parametrize("sobol", [0, 1])
+def test_fp32_risk_kernel_variants_within_tenth_of_stderr(eng, prod, sobol):
+    """Every variant of the FP32 Dupire risk kernel (barrier or European payoff, mrg32k3a or
+    Sobol draws) against the FP64 form on the same paths: prices and risks within 0.1 Monte
+    Carlo standard error."""
+    from compfinance_gb300 import workloads as W
+    s, t, v = W.dupire_surface(60, 30)
+    u = W.UOC_BARRIER
+    eng.putDupire(W.DUPIRE_SPOT, s, t, v, W.DUPIRE_MAXDT, "var60")
+    if prod == "uoc":
+        eng.putBarrier(u["strike"], u["barrier"], u["maturity"], u["monitor_freq"], u["smooth"], 0, "var_p")
+    else:
+        eng.putEuropean(110.0, 2.0, 2.0, "var_p")
+    n = 1 << 17
+    se = _se_fp64(eng, "var60", "var_p", n)
+    r64 = eng.AADriskOne("var60", "var_p", num(sobol, n, "fp64"))
+    r32 = eng.AADriskOne("var60", "var_p", num(sobol, n, "fp32"))
+    v64 = eng.value("var60", "var_p", num(0, n, "fp64"))
+    assert np.all(np.abs(r32["payoffValues"] - r64["payoffValues"]) <= 0.1 * v64["stderrs"])
+    mask = se > 1e-6 * np.abs(r64["risks"]).max()
+    assert mask.sum() > 50
+    assert np.all(np.abs(r32["risks"] - r64["risks"])[mask] <= 0.1 * se[mask])
+    assert np.all(np.abs(r32["risks"] - r64["risks"])[~mask] <= 1e-6 * np.abs(r64["risks"]).max())
+
+
+def test_fp32_risk_kernel_agrees_with_generic_kernel(eng, monkeypatch):
+    """The specialised FP32 Dupire risk kernel and the generic FP32 kernel (CF_FAST32=0)
+    compute the same paths with different roundings: both within 0.1 standard error."""
+    from compfinance_gb300 import workloads as W
+    s, t, v = W.dupire_surface(60, 30)
+    u = W.UOC_BARRIER
+    eng.putDupire(W.DUPIRE_SPOT, s, t, v, W.DUPIRE_MAXDT, "gen60")
+    eng.putBarrier(u["strike"], u["barrier"], u["maturity"], u["monitor_freq"], u["smooth"], 0, "gen_uoc")
+    n = 1 << 17
+    se = _se_fp64(eng, "gen60", "gen_uoc", n)
+    fast = eng.AADriskOne("gen60", "gen_uoc", num(0, n, "fp32"))
+    monkeypatch.setenv("CF_FAST32", "0")
+    generic = eng.AADriskOne("gen60", "gen_uoc", num(0, n, "fp32"))
+    monkeypatch.delenv("CF_FAST32")
+    mask = se > 1e-6 * np.abs(generic["risks"]).max()
+    assert np.all(np.abs(fast["risks"] - generic["risks"])[mask] <= 0.1 * se[mask])
+    assert abs(fast["payoffValues"][0] - generic["payoffValues"][0]) <= 1e-5 * abs(generic["payoffValues"][0])
+
+
+def test_fp32_risk_kernel_small_and_odd_path_counts(mc_eng):
+    """Partial units, partial warps and partial blocks of the FP32 risk kernel: FP32 against
+    FP64 on the same few paths, within FP32 rounding of the path arithmetic."""
+    eng, d = mc_eng
+    for n in (1, 2, 3, 31, 33, 257, 1001):
+        for sob in (0, 1):
+            r64 = eng.AADriskOne("dup60x30", "uoc", num(sob, n, "fp64"))
+            r32 = eng.AADriskOne("dup60x30", "uoc", num(sob, n, "fp32"))
+            scale = max(np.abs(r64["risks"]).max(), 1e-3)
+            assert np.abs(r32["risks"] - r64["risks"]).max() <= 5e-3 * scale, (n, sob)
+            assert abs(r32["payoffValues"][0] - r64["payoffValues"][0]) <= 1e-3 * max(abs(r64["payoffValues"][0]), 1e-3)

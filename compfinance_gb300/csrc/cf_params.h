@@ -129,6 +129,11 @@ struct McParams
                           // narrower than 2/3 of the smallest knot spacing (at most one knot each)
     int nBucketsF;
     float bX0F, bInvWF;
+    // Node adjoints are rounded to units of 2^-nodeShiftF (<= FIX_HI_SHIFT), chosen per plan so
+    // that an int32 shared slab word cannot overflow within one unit round; each block also
+    // keeps an int64 node slab in the scratch buffer at byte offset nodeSlabOffset.
+    int nodeShiftF;
+    long long nodeSlabOffset;
 };
 
 // Kernel configuration chosen by the host.
@@ -144,6 +149,9 @@ int launch_mc(const McLaunch& l, const McParams& p, void* stream);   // returns 
 int mc_smem_bytes(const McLaunch& l, const McParams& p, int stageY, size_t* bytes);
 int mc_occupancy(const McLaunch& l, size_t smem, int* blocksPerSM);
 int mc_scratch_fields(const McLaunch& l);   // reverse-sweep scratch fields of a risk launch
+// Bytes of a risk launch's scratch buffer: the fields [field][point][thread] for grid*128
+// threads, then (dupire_risk32) one int64 node slab per block.  Sets p.nodeSlabOffset.
+size_t mc_scratch_bytes(const McLaunch& l, McParams& p, long long grid);
 // Whether a (model, product, precision, mode) launch of this plan runs dupire_risk32
 // (CF_FAST32=0 in the environment selects the generic kernel instead).
 int mc_use_fast32(const McParams& plan, int prod, int fp32, int risk);

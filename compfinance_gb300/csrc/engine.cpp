@@ -406,8 +406,15 @@ int Context::buildPlan(const ModelDesc& m, const ProductDesc& pd, Plan& plan)
             bool evOk = evAtStep[n] == plan.nEv - 1;
             if (pd.kind == PROD_EUROPEAN)
                 for (int i = 0; i < n; ++i) evOk = evOk && evAtStep[i] < 0;
+            // node slab unit: a word receives per unit round at most 256 paths x (steps touching
+            // its time column) contributions, each below 512 x (largest time weight) in value
+            double wMax = 0.0;
+            for (int i = 0; i < n; ++i) wMax = std::max(wMax, std::max(cAv[i], cBv[i]));
+            const double perWord = 256.0 * sMax * 512.0 * std::max(wMax, 1e-300);
+            const int shift = int(std::floor(std::log2(1073741824.0 / perWord)));  // one bit of margin
+            P.nodeShiftF = std::min(FIX_HI_SHIFT, shift);
             P.fast32 = (pd.kind == PROD_UOC || pd.kind == PROD_EUROPEAN) && evOk && nS <= 510 && minGap > 0 &&
-                       range / nBf <= minGap / 1.5;
+                       range / nBf <= minGap / 1.5 && shift >= 4;
             P.nBucketsF = nBf;
             P.bX0F = Xf[0];
             P.bInvWF = float(1.0 / wf);
@@ -639,8 +646,7 @@ int Context::enqueue(Slot& slot, Plan& plan, const cf_num_param& num, bool risk,
         if (grid * 128 > maxThreads) grid = std::max(1LL, maxThreads / 128);
         l.grid = int(grid);
         p.scratchThreads = grid * 128;
-        const size_t bytes = size_t(p.scratchFields) * size_t(plan.nSteps + 1) * size_t(p.scratchThreads) *
-                             (fp32 ? 4 : 8);
+        const size_t bytes = mc_scratch_bytes(l, p, grid);
         if ((rc = slot.scratch.ensure(bytes))) return rc;
         p.scratch = slot.scratch.ptr;
     }
@@ -679,6 +685,7 @@ size_t Context::footprint(const Plan& plan, const cf_num_param& num, bool risk) 
     const int fields = plan.prod == PROD_EUROPEANS ? 1 + 3 * NP : mc_scratch_fields(l);
     size_t b = size_t(plan.nParam + 2 * plan.nPay + 2) * 16 + size_t(plan.nPay) * 12 + 4096;
     if (risk) b += size_t(fields) * size_t(plan.nSteps + 1) * size_t(threads) * (fp32 ? 4 : 8);
+    if (risk && l.fast) b += size_t((threads + 127) / 128) * size_t(plan.base.nS) * size_t(plan.base.nT) * 8 + 256;
     if (plan.prod == PROD_EUROPEANS && risk) b += size_t(plan.nPay + plan.nEv) * size_t(plan.nParam) * 16;
     return b;
 }

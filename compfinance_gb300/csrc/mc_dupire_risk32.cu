@@ -12,13 +12,16 @@
 //     exactly the operations of the forward.
 //  2. compaction: paths whose adjoint seed is zero (knocked out, or out of the money at
 //     maturity) contribute nothing to any risk; the block lists the others.
-//  3. reverse: the listed paths, one per thread, are swept back from maturity to today in
-//     lock step (one __syncthreads per step).  Local-vol adjoints of step s go into per-warp
-//     rows of int32 words (units of 2^-ROW_SHIFT, one native shared add per contribution);
-//     after the step, thread j moves spot j of the four rows into the node slab, which it
-//     alone owns, scaled by the step's integer time weights: plain loads and stores, no
-//     64-bit atomics.  Each contribution is rounded once, so every sum is independent of how
-//     paths are grouped into warps, blocks and launches.
+//  3. reverse: each listed path is swept back from maturity to today by one thread, with no
+//     block barrier inside the sweep.  The adjoint of each local-vol value the step used is
+//     split over its two spot knots and, with the step's time weights, over its two time
+//     columns, and each of the (up to) four parts is rounded once to an integer in units of
+//     2^-nodeShiftF and added (native 32-bit shared atomics) to an int32 slab of the
+//     local-vol nodes.  The host picks nodeShiftF so that no slab word can overflow within
+//     one unit round; after each round the slab is moved into a block-private int64 slab in
+//     global memory (each word owned by one thread), which is added to the accumulators
+//     once, at the end.  Each contribution is rounded once, so every sum is independent of
+//     how paths are grouped into warps, blocks and launches.
 #include <cuda_runtime.h>
 
 #include "cf_device.cuh"
@@ -37,18 +40,15 @@ constexpr int LO_SHIFT = T_BITS + 1;    // interval index in bits 23..31
 // are round(t 2^22): no conversion instruction either way
 constexpr unsigned TWO_BITS = 0x40000000u;         // bits of 2.0f
 constexpr float T_MAX = 1.0f - 1.0f / 4194304.0f;  // t + 2 stays below 3
-// A row word receives at most 32 contributions per step (one path per lane), each below
-// ROW_MAX32 * 2^ROW_SHIFT = 2^25 in magnitude: the word stays below 2^30.
-constexpr float ROW_MAX32 = 512.0f;
-constexpr int KSTEP = 1;                // reverse steps per block barrier (rows per group)
-constexpr long long SLAB_LIMIT = 1LL << 61;  // node slab words move to global beyond this
+// Contributions with |adjoint| >= AV_MAX go exactly to the global accumulators instead of
+// the int32 slab (the host's choice of nodeShiftF assumes this bound).
+constexpr float AV_MAX = 512.0f;
 
 __host__ __device__ inline size_t a16(size_t x) { return (x + 15) & ~size_t(15); }
 
 struct R32Layout
 {
-    size_t slab, node, rows, xs, ir, bucket, listIdx, listAx, listAl, cnt, base, total;
-    int rowPitch;
+    size_t slab, node, xs, ir, bucket, listIdx, listAx, listAl, cnt, stepc, base, total;
 };
 
 __host__ __device__ inline R32Layout r32_layout(int rng, const McParams& p)
@@ -57,11 +57,8 @@ __host__ __device__ inline R32Layout r32_layout(int rng, const McParams& p)
     size_t off = 0;
     L.slab = off;
     off += a16(size_t(4 + 2 * p.nPay + 2) * 16);
-    L.node = off;
-    off += a16(size_t(p.nS) * p.nT * 8);
-    L.rowPitch = (p.nS + 2) & ~1;  // nS + 1 words (the last interval's right node), even
-    L.rows = off;
-    off += a16(size_t(2 * KSTEP) * RW * L.rowPitch * 4);
+    L.node = off;  // int32 local-vol node slab of the current unit round
+    off += a16(size_t(p.nS) * p.nT * 4);
     L.xs = off;
     off += a16(size_t(p.nS + 2) * 4);
     L.ir = off;
@@ -76,6 +73,8 @@ __host__ __device__ inline R32Layout r32_layout(int rng, const McParams& p)
     off += a16(size_t(2 * RB) * 4);
     L.cnt = off;
     off += 16;
+    L.stepc = off;  // (colA, colB, weight A, weight B in units of 2^-nodeShiftF) per step
+    off += a16(size_t(p.nSteps) * 16);
     L.base = off;
     if (rng == RNG_SOBOL) off += a16(size_t(RW) * (size_t(p.nSteps) | 1) * 4);
     L.total = off;
@@ -91,8 +90,7 @@ __global__ void __launch_bounds__(RB, 8) dupire_risk32(const McParams p)
     const R32Layout L = r32_layout(RNGK, p);
     long long* slab = reinterpret_cast<long long*>(smem + L.slab);  // [0,2) spot adjoint, payoffs from 8
     long long* paySlab = slab + 8;
-    long long* node = reinterpret_cast<long long*>(smem + L.node);
-    int* rows = reinterpret_cast<int*>(smem + L.rows);              // [2 KSTEP][RW][rowPitch]
+    int* node = reinterpret_cast<int*>(smem + L.node);
     float* sXs = reinterpret_cast<float*>(smem + L.xs);
     float2* sIr = reinterpret_cast<float2*>(smem + L.ir);
     int* sBucket = reinterpret_cast<int*>(smem + L.bucket);
@@ -100,16 +98,26 @@ __global__ void __launch_bounds__(RB, 8) dupire_risk32(const McParams p)
     float* listAx = reinterpret_cast<float*>(smem + L.listAx);
     float* listAl = reinterpret_cast<float*>(smem + L.listAl);
     int* cnt = reinterpret_cast<int*>(smem + L.cnt);
+    int4* stepc = reinterpret_cast<int4*>(smem + L.stepc);
 
     const int tid = threadIdx.x, lane = tid & 31, wib = tid >> 5;
-    const int nS = p.nS, nT = p.nT, nSteps = p.nSteps, nPay = p.nPay;
-    const int rowPitch = L.rowPitch;
+    const int nS = p.nS, nT = p.nT, nSteps = p.nSteps, nPay = p.nPay, nNodes = nS * nT;
+    // block-private int64 node slab in global memory, after the scratch fields; word i is
+    // read and written only by thread i mod RB
+    long long* gnode = reinterpret_cast<long long*>(static_cast<char*>(p.scratch) + p.nodeSlabOffset) +
+                       size_t(blockIdx.x) * nNodes;
+    const float wScale = ldexpf(1.0f, p.nodeShiftF);
     for (int i = tid; i < 2 * (4 + 2 * nPay + 2); i += RB) slab[i] = 0;
-    for (int i = tid; i < nS * nT; i += RB) node[i] = 0;
-    for (int i = tid; i < 2 * KSTEP * RW * rowPitch; i += RB) rows[i] = 0;
+    for (int i = tid; i < nNodes; i += RB)
+    {
+        node[i] = 0;
+        gnode[i] = 0;
+    }
     for (int i = tid; i < nS + 2; i += RB) sXs[i] = p.xsF[i];
     for (int i = tid; i < nS + 1; i += RB) sIr[i] = make_float2(p.irF[2 * i], p.irF[2 * i + 1]);
     for (int i = tid; i < p.nBucketsF; i += RB) sBucket[i] = p.bucketF[i];
+    for (int i = tid; i < nSteps; i += RB)
+        stepc[i] = make_int4(p.colA[i], p.colB[i], __float_as_int(p.cAf[i] * wScale), __float_as_int(p.cBf[i] * wScale));
     __syncthreads();
 
     const float2* td = reinterpret_cast<const float2*>(p.tdF);
@@ -210,7 +218,7 @@ __global__ void __launch_bounds__(RB, 8) dupire_risk32(const McParams p)
         for (int s = 0; s < nSteps; ++s)
         {
             const float g = gen(s);
-            scr[F_G * rowStride + s * Ti + myCol] = g;
+            __stcs(scr + F_G * rowStride + s * Ti + myCol, g);  // streamed: read once, in the reverse
             const float2* trow = td + size_t(s) * tPitch;
 #pragma unroll
             for (int a = 0; a < NP; ++a)
@@ -223,8 +231,8 @@ __global__ void __launch_bounds__(RB, 8) dupire_risk32(const McParams p)
                 const unsigned tq = __float_as_uint(t2) & T_MASK;
                 const float2 yd = __ldg(trow + lo);
                 const float v = fmaf(yd.y, t2 - 2.0f, yd.x);
-                reinterpret_cast<unsigned*>(scr)[(F_W + a) * rowStride + s * Ti + myCol] =
-                    (unsigned(lo) << LO_SHIFT) | (flag[a] ? BAND_BIT : 0u) | tq;
+                __stcs(reinterpret_cast<unsigned*>(scr) + (F_W + a) * rowStride + s * Ti + myCol,
+                       (unsigned(lo) << LO_SHIFT) | (flag[a] ? BAND_BIT : 0u) | tq);
                 flag[a] = 0;  // the flag of point s + 1 is set by its date, if any
                 x[a] += v * (-0.5f * v + ga);
             }
@@ -275,25 +283,15 @@ __global__ void __launch_bounds__(RB, 8) dupire_risk32(const McParams p)
     };
 
     // contribution c (units of 1) to spot j of step s's vol row: exact global fixed point when
-    // too large for a row word
+    // too large for the slab
     auto bigAdd = [&](int s, int j, float c) {
         fix_add(&p.acc[2 * (1 + j * nT + __ldg(p.colA + s))], c * __ldg(p.cAf + s));
         const float cb = __ldg(p.cBf + s);
         if (cb != 0.0f) fix_add(&p.acc[2 * (1 + j * nT + __ldg(p.colB + s))], c * cb);
     };
-    // thread-owned node slab word += v (units of 2^-NODE_SHIFT)
-    auto nodeAdd = [&](int idx, long long v) {
-        long long n = node[idx] + v;
-        if (n > SLAB_LIMIT || n < -SLAB_LIMIT)
-        {
-            node_flush(&p.acc[2 * (1 + idx)], n);
-            n = 0;
-        }
-        node[idx] = n;
-    };
 
     // ---------------------------------------------------------------------------------
-    // Compaction and reverse sweep of one unit round (block-uniform).
+    // Compaction and reverse sweep of one unit round, then the round's slab -> gnode.
     // ---------------------------------------------------------------------------------
     auto reverse = [&]() {
         const unsigned b0 = __ballot_sync(0xffffffffu, live[0]);
@@ -324,105 +322,95 @@ __global__ void __launch_bounds__(RB, 8) dupire_risk32(const McParams p)
             listAl[pos] = alOut[NP - 1];
         }
         __syncthreads();
-        const int nPass = (total + RB - 1) / RB;
-        for (int pass = 0; pass < nPass; ++pass)
+        for (int idx = tid; idx < total; idx += RB)
         {
-            const int idx = pass * RB + tid;
-            const bool has = idx < total;
-            int a = 0, col = 0;
-            float ax = 0.0f, aAl = 0.0f;
-            if (has)
-            {
-                const int e = listIdx[idx];
-                a = e & 1;
-                col = int(blockIdx.x) * RB + (e >> 1);
-                ax = listAx[idx];
-                aAl = listAl[idx];
-            }
+            const int e = listIdx[idx];
+            const int a = e & 1;
+            const int col = int(blockIdx.x) * RB + (e >> 1);
+            float ax = listAx[idx], aAl = listAl[idx];
             const unsigned* sw = reinterpret_cast<const unsigned*>(scr) + (F_W + a) * rowStride + col;
             const float* sg = scr + F_G * rowStride + col;
-            int* myRow = rows + wib * rowPitch;
             unsigned wNext = 0;  // packed word of the step after s: band flag of point s + 1
-            // steps nSteps-1 .. 0 in groups of KSTEP; group g uses row sets (g & 1) KSTEP + k
-            for (int s0 = nSteps - 1, g = 0; s0 >= 0; s0 -= KSTEP, ++g)
+            // the step words and Gaussians are loaded two steps ahead
+            unsigned wq0 = __ldcs(sw + (nSteps - 1) * Ti), wq1 = 0;
+            float gq0 = __ldcs(sg + (nSteps - 1) * Ti), gq1 = 0.0f;
+            if (nSteps >= 2)
             {
-                const int kEnd = s0 + 1 < KSTEP ? s0 + 1 : KSTEP;
-                const int set0 = (g & 1) * KSTEP;
-                for (int k = 0; k < kEnd; ++k)
-                {
-                    const int s = s0 - k;
-                    if (!has) continue;
-                    if (UOC && (wNext & BAND_BIT))
-                    {
-                        const int i = s + 1;
-                        const float before = scr[(F_B + a) * rowStride + i * Ti + col];
-                        const float S = scr[(F_S + a) * rowStride + i * Ti + col];
-                        const float aF = aAl * before * invTwo;
-                        aAl *= (barSmooth - S) / twoSmooth;
-                        ax += aF * S;
-                    }
-                    const unsigned W = sw[s * Ti];
-                    const float g1 = sg[s * Ti];
-                    const float ga = a ? -g1 : g1;
-                    const int lo = int(W >> LO_SHIFT);
-                    const float t = __uint_as_float(TWO_BITS | (W & T_MASK)) - 2.0f;
-                    const float2 yd = __ldg(td + size_t(s) * tPitch + lo);
-                    const float2 ir = sIr[lo];
-                    const float v = fmaf(yd.y, t, yd.x);
-                    const float av = ax * (ga - v);      // d x_{s+1} / d v = g - v
-                    ax += av * (yd.y * ir.y);            // d x_{s+1} / d x_s = 1 + (g - v) dv/dx
-                    if (av != 0.0f)
-                    {
-                        const int jl = lo - (lo > 0 ? 1 : 0);
-                        const bool inner = lo > 0 && lo < nS;  // two nodes; one at flat ends
-                        const float cR = av * t, cL = av - cR;
-                        if (fabsf(av) < ROW_MAX32)
-                        {
-                            int* row = myRow + (set0 + k) * RW * rowPitch;
-                            atomicAdd(&row[jl], __float2int_rn(cL * 65536.0f));
-                            if (inner && cR != 0.0f) atomicAdd(&row[jl + 1], __float2int_rn(cR * 65536.0f));
-                        }
-                        else
-                        {
-                            bigAdd(s, jl, cL);
-                            if (inner && cR != 0.0f) bigAdd(s, jl + 1, cR);
-                        }
-                    }
-                    wNext = W;
-                }
-                __syncthreads();
-                // the group's rows -> node slab; spot j = 4 q + w belongs to thread (w, q mod 32)
-                for (int k = 0; k < kEnd; ++k)
-                {
-                    const int s = s0 - k;
-                    const long long WA = __ldg(p.wAi + s), WB = __ldg(p.wBi + s);
-                    const int ca = __ldg(p.colA + s), cb = __ldg(p.colB + s);
-                    int* rs = rows + (set0 + k) * RW * rowPitch;
-                    for (int j = 4 * lane + wib; j < nS; j += 4 * 32)
-                    {
-                        int* r = rs + j;
-                        const int r0 = r[0], r1 = r[rowPitch], r2 = r[2 * rowPitch], r3 = r[3 * rowPitch];
-                        if (r0 | r1 | r2 | r3)
-                        {
-                            r[0] = r[rowPitch] = r[2 * rowPitch] = r[3 * rowPitch] = 0;
-                            const long long sum = (long long)r0 + r1 + r2 + r3;
-                            nodeAdd(j * nT + ca, WA * sum);
-                            if (WB != 0) nodeAdd(j * nT + cb, WB * sum);
-                        }
-                    }
-                }
+                wq1 = __ldcs(sw + (nSteps - 2) * Ti);
+                gq1 = __ldcs(sg + (nSteps - 2) * Ti);
             }
-            if (has)
+            for (int s = nSteps - 1; s >= 0; --s)
             {
-                if (UOC && (wNext & BAND_BIT))  // band at today's date
+                if (UOC && (wNext & BAND_BIT))
                 {
-                    const float before = scr[(F_B + a) * rowStride + col];
-                    const float S = scr[(F_S + a) * rowStride + col];
-                    ax += aAl * before * invTwo * S;
+                    const int i = s + 1;
+                    const float before = scr[(F_B + a) * rowStride + i * Ti + col];
+                    const float S = scr[(F_S + a) * rowStride + i * Ti + col];
+                    const float aF = aAl * before * invTwo;
+                    aAl *= (barSmooth - S) / twoSmooth;
+                    ax += aF * S;
                 }
-                fix_add(&slab[0], ax / spot);  // x_0 = log(spot)
+                const unsigned W = wq0;
+                const float g1 = gq0;
+                wq0 = wq1;
+                gq0 = gq1;
+                if (s >= 2)
+                {
+                    wq1 = __ldcs(sw + (s - 2) * Ti);
+                    gq1 = __ldcs(sg + (s - 2) * Ti);
+                }
+                const float ga = a ? -g1 : g1;
+                const int lo = int(W >> LO_SHIFT);
+                const float t = __uint_as_float(TWO_BITS | (W & T_MASK)) - 2.0f;
+                const float2 yd = __ldg(td + size_t(s) * tPitch + lo);
+                const float2 ir = sIr[lo];
+                const float v = fmaf(yd.y, t, yd.x);
+                const float av = ax * (ga - v);      // d x_{s+1} / d v = g - v
+                ax += av * (yd.y * ir.y);            // d x_{s+1} / d x_s = 1 + (g - v) dv/dx
+                if (av != 0.0f)
+                {
+                    const int jl = lo - (lo > 0 ? 1 : 0);
+                    const bool inner = lo > 0 && lo < nS;  // two spot knots; one at the flat ends
+                    const float cR = av * t, cL = av - cR;
+                    if (fabsf(av) < AV_MAX)
+                    {
+                        const int4 sc = stepc[s];
+                        const float wa = __int_as_float(sc.z), wb = __int_as_float(sc.w);
+                        int* nl = node + jl * nT;
+                        atomicAdd(nl + sc.x, __float2int_rn(cL * wa));
+                        if (wb != 0.0f) atomicAdd(nl + sc.y, __float2int_rn(cL * wb));
+                        if (inner && cR != 0.0f)
+                        {
+                            atomicAdd(nl + nT + sc.x, __float2int_rn(cR * wa));
+                            if (wb != 0.0f) atomicAdd(nl + nT + sc.y, __float2int_rn(cR * wb));
+                        }
+                    }
+                    else
+                    {
+                        bigAdd(s, jl, cL);
+                        if (inner && cR != 0.0f) bigAdd(s, jl + 1, cR);
+                    }
+                }
+                wNext = W;
             }
-            __syncthreads();
+            if (UOC && (wNext & BAND_BIT))  // band at today's date
+            {
+                const float before = scr[(F_B + a) * rowStride + col];
+                const float S = scr[(F_S + a) * rowStride + col];
+                ax += aAl * before * invTwo * S;
+            }
+            fix_add(&slab[0], ax / spot);  // x_0 = log(spot)
+        }
+        __syncthreads();
+        // the round's slab -> this thread's words of the block's int64 slab
+        for (int i = tid; i < nNodes; i += RB)
+        {
+            const int v = node[i];
+            if (v)
+            {
+                node[i] = 0;
+                gnode[i] += v;
+            }
         }
     };
 
@@ -475,7 +463,13 @@ __global__ void __launch_bounds__(RB, 8) dupire_risk32(const McParams p)
 
     __syncthreads();
     if (tid == 0) fix_flush(&p.acc[0], &slab[0]);
-    for (int i = tid; i < nS * nT; i += RB) node_flush(&p.acc[2 * (1 + i)], node[i]);
+    // node words in units of 2^-nodeShiftF (nodeShiftF <= FIX_HI_SHIFT): exact in the hi word
+    for (int i = tid; i < nNodes; i += RB)
+    {
+        const long long v = gnode[i];
+        if (v) atomicAdd(reinterpret_cast<unsigned long long*>(&p.acc[2 * (1 + i)]),
+                         (unsigned long long)(v << (FIX_HI_SHIFT - p.nodeShiftF)));
+    }
     for (int i = tid; i < 2 * nPay + 2; i += RB) fix_flush(&p.acc[2 * (p.nRisk + i)], &paySlab[2 * i]);
 }
 

@@ -40,6 +40,18 @@ int mc_scratch_fields(const McLaunch& l)
     return 1 + NP + (l.prod == PROD_UOC ? NP : 0);
 }
 
+size_t mc_scratch_bytes(const McLaunch& l, McParams& p, long long grid)
+{
+    const size_t fields = size_t(mc_scratch_fields(l)) * size_t(p.nSteps + 1) * size_t(grid) * 128 * (l.fp32 ? 4 : 8);
+    if (!l.fast)
+    {
+        p.nodeSlabOffset = 0;
+        return fields;
+    }
+    p.nodeSlabOffset = (long long)((fields + 255) & ~size_t(255));
+    return size_t(p.nodeSlabOffset) + size_t(grid) * size_t(p.nS) * size_t(p.nT) * 8;
+}
+
 int mc_use_fast32(const McParams& plan, int prod, int fp32, int risk)
 {
     if (!plan.fast32 || !fp32 || !risk || (prod != PROD_UOC && prod != PROD_EUROPEAN)) return 0;

@@ -155,12 +155,17 @@ extern "C" int cf_aad_risk_aggregate_noalloc(cf_context* ctx, const char* modelI
         if ((rc = mc_occupancy(l, smem, &occ)) || occ < 1) return fail_c(CF_E_SHAPE, "noalloc: kernel does not fit");
     }
     p.scratchFields = mc_scratch_fields(l);
+    // scratch per block: the reverse-sweep fields of 128 threads, plus the FP32 kernel's
+    // int64 node slab (and 256 bytes of alignment between the two regions)
     const size_t perThread = size_t(p.scratchFields) * size_t(plan->nSteps + 1) * (fp32 ? 4 : 8);
-    const long long fitBlocks = (long long)((CF_NOALLOC_BYTES - offScr) / (perThread * 128));
+    const size_t perBlock = perThread * 128 + (l.fast ? size_t(p.nS) * size_t(p.nT) * 8 : 0);
+    const long long fitBlocks = (long long)((CF_NOALLOC_BYTES - offScr - 256) / perBlock);
     if (fitBlocks < 1) return fail_c(CF_E_SHAPE, "noalloc: one block of reverse-sweep scratch exceeds the arena");
     const long long threadsNeeded = sobol ? (p.nPath / 32 + 1) * 32 : (p.nPath + 1) / 2;
     long long grid = std::min<long long>((threadsNeeded + 127) / 128, (long long)c.numSMs * occ);
     grid = std::max(1LL, std::min(grid, fitBlocks));
+    if (mc_scratch_bytes(l, p, grid) > CF_NOALLOC_BYTES - offScr)
+        return fail_c(CF_E_SHAPE, "noalloc: reverse-sweep scratch exceeds the arena");
     l.grid = int(grid);
     l.smem = smem;
     p.scratchThreads = grid * 128;

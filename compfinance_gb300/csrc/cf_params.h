@@ -82,7 +82,8 @@ struct McParams
     const int* wBi;
     int nodeFlushUnits;   // FP32 risk: units per thread between node slab flushes (>= 1)
     int nodeDirect;       // FP32 risk: 1 = add row products straight to the global accumulators
-    int stageY;           // 1: stage Y into shared memory (cp.async.bulk)
+    int stageY;           // 1: stage Y into shared memory (cp.async.bulk); in dupire_risk32,
+                          // stage the inverse-normal table instead
     // Bucket index of the log-spot grid: bucket b of nBuckets equal slices of [X0, X_last]
     // holds the upper_bound of its left edge, a starting guess for the interpolation search.
     int nBuckets;
@@ -134,6 +135,7 @@ struct McParams
     // keeps an int64 node slab in the scratch buffer at byte offset nodeSlabOffset.
     int nodeShiftF;
     long long nodeSlabOffset;
+    const float* invnF;   // [512][4] piecewise-cubic inverse normal of the launch's generator
 };
 
 // Kernel configuration chosen by the host.

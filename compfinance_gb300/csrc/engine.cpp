@@ -515,6 +515,14 @@ int Context::init(int dev)
     CF_CUDA(cudaMemcpy(static_cast<char*>(jump.ptr) + sizeof(A), B, sizeof(B), cudaMemcpyHostToDevice));
     jumpA = static_cast<const unsigned long long*>(jump.ptr);
     jumpB = jumpA + 64 * 9;
+    // uniforms: mrg32k3a d / (m1 + 1) (mrg32k3a.h:52,78-79), Sobol s * 2.3283064365387e-10 (sobol.h:26)
+    std::vector<float> tab(2 * size_t(INVN_PIECES) * 4);
+    inv_normal_table(4294967088.0, tab.data());
+    inv_normal_table(1.0 / 2.3283064365387e-10, tab.data() + size_t(INVN_PIECES) * 4);
+    if ((rc = invn.ensure(tab.size() * sizeof(float)))) return rc;
+    CF_CUDA(cudaMemcpy(invn.ptr, tab.data(), tab.size() * sizeof(float), cudaMemcpyHostToDevice));
+    invnMrg = static_cast<const float*>(invn.ptr);
+    invnSobol = invnMrg + size_t(INVN_PIECES) * 4;
     main.stream = stream;
     return CF_OK;
 }
@@ -568,6 +576,7 @@ int Context::enqueue(Slot& slot, Plan& plan, const cf_num_param& num, bool risk,
     p.seed2 = unsigned(num.seed2);
     p.mrgJumpA = jumpA;
     p.mrgJumpB = jumpB;
+    p.invnF = sobol ? invnSobol : invnMrg;
     p.nRisk = risk ? plan.nParam : 0;
     p.nAcc = p.nRisk + 2 * plan.nPay + 2;
     // weights (double and float copies), accumulators and the error flag share one buffer
@@ -602,8 +611,17 @@ int Context::enqueue(Slot& slot, Plan& plan, const cf_num_param& num, bool risk,
     l.fast = mc_use_fast32(plan.base, plan.prod, l.fp32, l.risk);
     if (l.fast)
     {
+        // the inverse-normal table goes to shared memory when that costs no occupancy
+        p.stageY = 0;
         mc_smem_bytes(l, p, 0, &smem0);
         if (smem0 > 200 * 1024 || mc_occupancy(l, smem0, &occ0) || occ0 < 1) l.fast = 0;
+        else
+        {
+            p.stageY = 1;
+            mc_smem_bytes(l, p, 1, &smem1);
+            if (mc_occupancy(l, smem1, &occ1) || occ1 < occ0) p.stageY = 0;
+            else smem0 = smem1;
+        }
     }
     if (!l.fast)
     {
@@ -626,7 +644,7 @@ int Context::enqueue(Slot& slot, Plan& plan, const cf_num_param& num, bool risk,
         if (env && env[0] == '0') stage = 0;
         if (env && env[0] == '1' && occ1 > 0) stage = 1;
     }
-    p.stageY = stage;
+    if (!l.fast) p.stageY = stage;
     l.smem = stage ? smem1 : smem0;
     const int occ = stage ? occ1 : occ0;
     if (occ < 1) return fail(CF_E_SHAPE, "kernel does not fit on an SM (shared memory " + std::to_string(l.smem) + ")");

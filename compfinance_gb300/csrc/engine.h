@@ -120,6 +120,9 @@ struct Context
     DevBuf jump;
     const unsigned long long* jumpA = nullptr;
     const unsigned long long* jumpB = nullptr;
+    DevBuf invn;  // piecewise-cubic inverse normal tables of the FP32 kernels: mrg32k3a, Sobol
+    const float* invnMrg = nullptr;
+    const float* invnSobol = nullptr;
     Slot main;
     unsigned long long h2d = 0, d2h = 0;  // cumulative transfer bytes
 

@@ -171,4 +171,72 @@ double merton_price(double spot, double strike, double vol, double mat, double i
     return res;
 }
 
+double inv_normal_bsm(double p)
+{
+    const bool sup = p > 0.5;
+    const double up = sup ? 1.0 - p : p;
+    const double x = up - 0.5;
+    if (std::fabs(x) < 0.42)
+    {
+        const double r = x * x;
+        const double v = x * (((-25.44106049637 * r + 41.39119773534) * r + -18.61500062529) * r + 2.50662823884) /
+                         ((((3.13082909833 * r + -21.06224101826) * r + 23.08336743743) * r + -8.47351093090) * r + 1.0);
+        return sup ? -v : v;
+    }
+    double r = std::log(-std::log(up));
+    r = 0.3374754822726147 +
+        r * (0.9761690190917186 +
+             r * (0.1607979714918209 +
+                  r * (0.0276438810333863 +
+                       r * (0.0038405729373609 +
+                            r * (0.0003951896511919 +
+                                 r * (0.0000321767881768 + r * (0.0000002888167364 + r * 0.0000003960315187)))))));
+    return sup ? r : -r;
+}
+
+void inv_normal_table(double denom, float* out)
+{
+    const int nSub = 1 << INVN_SUB_BITS;
+    const double pi = 3.14159265358979323846;
+    for (int b = 0; b < 32; ++b)
+        for (int sub = 0; sub < nSub; ++sub)
+        {
+            // piece: up in 2^b (1 + (sub + z) / nSub), z in [0, 1)
+            double z[4], y[4];
+            for (int i = 0; i < 4; ++i)
+            {
+                z[i] = 0.5 - 0.5 * std::cos((2 * i + 1) * pi / 8.0);
+                const double up = std::ldexp(1.0 + (sub + z[i]) / nSub, b);
+                y[i] = inv_normal_bsm(up / denom);
+            }
+            // cubic through the four nodes: Vandermonde solve by Gaussian elimination
+            double A[4][5];
+            for (int i = 0; i < 4; ++i)
+            {
+                double zk = 1.0;
+                for (int k = 0; k < 4; ++k)
+                {
+                    A[i][k] = zk;
+                    zk *= z[i];
+                }
+                A[i][4] = y[i];
+            }
+            for (int c = 0; c < 4; ++c)
+            {
+                int piv = c;
+                for (int r = c + 1; r < 4; ++r)
+                    if (std::fabs(A[r][c]) > std::fabs(A[piv][c])) piv = r;
+                for (int k = 0; k < 5; ++k) std::swap(A[c][k], A[piv][k]);
+                for (int r = 0; r < 4; ++r)
+                    if (r != c)
+                    {
+                        const double f = A[r][c] / A[c][c];
+                        for (int k = c; k < 5; ++k) A[r][k] -= f * A[c][k];
+                    }
+            }
+            float* o = out + 4 * (b * nSub + sub);
+            for (int k = 0; k < 4; ++k) o[k] = float(A[k][4] / A[k][k]);
+        }
+}
+
 }  // namespace cf

@@ -33,6 +33,20 @@ std::vector<uint32_t> sobol_dirs(int dims);
 // two mrg32k3a recurrences (mrg32k3a.h:319-358).
 void mrg_jump_tables(uint64_t A[64][9], uint64_t B[64][9]);
 
+// Beasley-Springer-Moro inverse normal (gaussians.h:47-87), in double.
+double inv_normal_bsm(double p);
+
+// Piecewise-cubic table of the inverse normal for the FP32 kernels.  A draw's lower-half
+// integer up in [1, 2^31] (the uniform is up / denom) is located by its leading bit (binade b
+// = 31 - clz(up), 32 of them) and the next INVN_SUB_BITS bits (sub-interval); within the
+// piece, z in [0, 1) is the fraction of the remaining bits.  Entry 4*(b * 2^SUB + sub) + k is
+// the coefficient of z^k of the cubic through the inverse normal at four Chebyshev nodes of
+// the piece (max error 1.2e-8 against the double-precision function).  The value is the
+// lower-half Gaussian (negative); the upper half is its negation.
+constexpr int INVN_SUB_BITS = 4;
+constexpr int INVN_PIECES = 32 << INVN_SUB_BITS;
+void inv_normal_table(double denom, float* out /* [INVN_PIECES][4] */);
+
 // Black-Scholes formula, Zelen-Severo normal CDF, implied vol, Merton (analytics.h:8-91).
 double normal_cdf(double x);
 double normal_dens(double x);

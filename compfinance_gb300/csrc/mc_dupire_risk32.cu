@@ -48,7 +48,7 @@ __host__ __device__ inline size_t a16(size_t x) { return (x + 15) & ~size_t(15);
 
 struct R32Layout
 {
-    size_t slab, node, xs, ir, bucket, listIdx, listAx, listAl, cnt, stepc, base, total;
+    size_t slab, node, xs, ir, bucket, listIdx, listAx, listAl, cnt, stepc, invn, base, total;
 };
 
 __host__ __device__ inline R32Layout r32_layout(int rng, const McParams& p)
@@ -75,6 +75,8 @@ __host__ __device__ inline R32Layout r32_layout(int rng, const McParams& p)
     off += 16;
     L.stepc = off;  // (colA, colB, weight A, weight B in units of 2^-nodeShiftF) per step
     off += a16(size_t(p.nSteps) * 16);
+    L.invn = off;   // piecewise-cubic inverse normal, 512 pieces (when staged: p.stageY)
+    if (p.stageY) off += size_t(512) * 16;
     L.base = off;
     if (rng == RNG_SOBOL) off += a16(size_t(RW) * (size_t(p.nSteps) | 1) * 4);
     L.total = off;
@@ -99,6 +101,7 @@ __global__ void __launch_bounds__(RB, 8) dupire_risk32(const McParams p)
     float* listAl = reinterpret_cast<float*>(smem + L.listAl);
     int* cnt = reinterpret_cast<int*>(smem + L.cnt);
     int4* stepc = reinterpret_cast<int4*>(smem + L.stepc);
+    float4* sInvn = reinterpret_cast<float4*>(smem + L.invn);
 
     const int tid = threadIdx.x, lane = tid & 31, wib = tid >> 5;
     const int nS = p.nS, nT = p.nT, nSteps = p.nSteps, nPay = p.nPay, nNodes = nS * nT;
@@ -116,6 +119,10 @@ __global__ void __launch_bounds__(RB, 8) dupire_risk32(const McParams p)
     for (int i = tid; i < nS + 2; i += RB) sXs[i] = p.xsF[i];
     for (int i = tid; i < nS + 1; i += RB) sIr[i] = make_float2(p.irF[2 * i], p.irF[2 * i + 1]);
     for (int i = tid; i < p.nBucketsF; i += RB) sBucket[i] = p.bucketF[i];
+    const float4* gInvn = reinterpret_cast<const float4*>(p.invnF);
+    const bool stageInvn = p.stageY != 0;
+    if (stageInvn)
+        for (int i = tid; i < 512; i += RB) sInvn[i] = gInvn[i];
     for (int i = tid; i < nSteps; i += RB)
         stepc[i] = make_int4(p.colA[i], p.colB[i], __float_as_int(p.cAf[i] * wScale), __float_as_int(p.cBf[i] * wScale));
     __syncthreads();
@@ -138,6 +145,19 @@ __global__ void __launch_bounds__(RB, 8) dupire_risk32(const McParams p)
     float* scr = reinterpret_cast<float*>(p.scratch);
     constexpr int F_G = 0, F_W = 1, F_B = 1 + NP, F_S = 1 + 2 * NP;
     const int myCol = int(blockIdx.x) * RB + tid;
+
+    // Gaussian of a lower-half integer draw up in [1, 2^31] (uniform up / denom of the
+    // generator; sup: the draw was in the upper half): the piece is the leading bit of up and
+    // the 4 bits after it, z the fraction of the remaining bits, the value a cubic in z.
+    auto gaussT = [&](unsigned up, bool sup) -> float {
+        const int lz = __clz(up);
+        const unsigned nrm = up << lz;  // leading one at bit 31
+        const int piece = ((31 - lz) << 4) | int((nrm >> 27) & 15u);
+        const float z = __uint_as_float(0x3F800000u | ((nrm << 5) >> 9)) - 1.0f;
+        const float4 c = stageInvn ? sInvn[piece] : __ldg(gInvn + piece);
+        const float g = fmaf(fmaf(fmaf(c.w, z, c.z), z, c.y), z, c.x);
+        return sup ? -g : g;
+    };
 
     // upper_bound of xs among the knots (exact: a bucket holds at most one knot, and the
     // bucket of xs computed in FP32 is off by at most one)
@@ -428,7 +448,11 @@ __global__ void __launch_bounds__(RB, 8) dupire_risk32(const McParams p)
         {
             const long long u = u0 + it;
             const int nAct = u < u1 ? ((2 * u + 1 < p.nPath) ? 2 : 1) : 0;
-            forward(nAct, [&](int) { return mrg_gauss<float>(mrg_next(st)); });
+            forward(nAct, [&](int) {
+                const unsigned d = mrg_next(st);   // in [1, m1]; uniform d / (m1 + 1)
+                const bool sup = d > 2147483544u;  // (m1 + 1) / 2
+                return gaussT(sup ? 4294967088u - d : d, sup);
+            });
             reverse();
         }
     }
@@ -455,7 +479,9 @@ __global__ void __launch_bounds__(RB, 8) dupire_risk32(const McParams p)
                 nAct = (n >= 1 && n <= p.nPath) ? 1 : 0;
             }
             forward(nAct, [&](int i) {
-                return sobol_gauss<float>(base[i] ^ sobol_state(p.sobolDir, nSteps, i, (unsigned long long)lane));
+                const unsigned sb = base[i] ^ sobol_state(p.sobolDir, nSteps, i, (unsigned long long)lane);
+                const bool sup = sb >= 2147483648u;
+                return gaussT(sup ? 0u - sb : (sb > 1u ? sb : 1u), sup);  // state 0 occurs only at index 0
             });
             reverse();
         }

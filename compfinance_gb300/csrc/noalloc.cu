@@ -129,6 +129,7 @@ extern "C" int cf_aad_risk_aggregate_noalloc(cf_context* ctx, const char* modelI
     p.seed2 = unsigned(num->seed2);
     p.mrgJumpA = c.jumpA;
     p.mrgJumpB = c.jumpB;
+    p.invnF = sobol ? c.invnSobol : c.invnMrg;
     p.nRisk = plan->nParam;
     p.nAcc = p.nRisk + 2 * plan->nPay + 2;
     // arena layout: weights | accumulators + error flag | results | scratch

@@ -35,7 +35,7 @@ METRIC = "AAD-risk paths/s (Dupire barrier), FP32 vs FP64 at equal error; serve 
 NPATH = 1 << 22
 GRID = (60, 30)
 FLOPS_PER_PATH_STEP = 53.0   # algorithmic FP work of value + adjoint per path-step (mrg32k3a)
-TRAFFIC_BYTES_PER_PATH_STEP = 10.54  # measured DRAM traffic of the FP32 risk launch per path-step
+TRAFFIC_BYTES_PER_PATH_STEP = 10.56  # measured DRAM traffic of the FP32 risk launch per path-step
 CONFIG = {
     "workload": "dupire_uoc_aad_risk_60x30_156steps_2^22paths_fp32path",
     "model": "Dupire local vol 60x30 (50-200 log-spaced x 0.1-3.0y), seeded synthetic surface",
@@ -296,7 +296,7 @@ def main():
     peak_fp32 = 152 * 128 * 2 * sm_max * 1e6 / 1e12
     achieved = FLOPS_PER_PATH_STEP * steps_tot / per_step / 1e12
     # DRAM bytes per launch: dram__bytes_read.sum + dram__bytes_write.sum of one ncu capture of
-    # this kernel at 2^20 paths, per path-step, times the path-steps of this launch (same grid,
+    # dupire_risk32 at 2^20 paths, per path-step, times the path-steps of this launch (same grid,
     # same scratch; the traffic grows with the path-steps)
     traffic = TRAFFIC_BYTES_PER_PATH_STEP * steps_tot if npath == NPATH else None
     out = {

@@ -138,7 +138,8 @@ def serving_leg(eng, n, seed):
     """Mixed request stream (seeded Poisson arrivals at 2,000 req/s; 40% BS values, 40% Dupire
     barrier risks of 2^16-2^20 paths on 20x10..120x60 grids with 12..520 steps, 20% European
     portfolio AADriskMulti), FP32 path form, 64 GB admission budget, 8 slots; then the same
-    requests one at a time through the synchronous entry points."""
+    requests all submitted at once (the server's batch throughput) and one at a time through the
+    synchronous entry points."""
     from compfinance_gb300.serve_stream import load_store, run_one_at_a_time, run_stream
     models, products = W.serving_store()
     load_store(eng, models, products)
@@ -147,16 +148,102 @@ def serving_leg(eng, n, seed):
         eng.shapes(r["model"], r["product"])
     run_stream(eng, W.serving_stream(n=64, rate=1e6, seed=seed + 1), slots=8)
     stats, makespan, status, _ = run_stream(eng, stream, slots=8, budget=64 << 30)
+    # batch: the same requests all submitted at once to the same server (its capacity)
+    bstats, bmakespan, _, _ = run_stream(eng, [dict(r, t=0.0) for r in stream], slots=8, budget=64 << 30)
     t_seq, steps = run_one_at_a_time(eng, stream)
     served = stats["pathStepsDone"] / makespan
+    batch_all = bstats["pathStepsDone"] / bmakespan
     batch = steps / t_seq
     return {"requests": n, "arrival_rate_req_s": 2000.0, "slots": 8, "hbm_budget_gb": 64,
             "completed": stats["completed"], "failed": stats["failed"], "rejected": stats["rejected"],
             "p50_ms": stats["p50Ms"], "p99_ms": stats["p99Ms"], "mean_ms": stats["meanMs"],
             "makespan_s": makespan, "served_path_steps_per_s": served,
+            "batch_makespan_s": bmakespan, "batch_path_steps_per_s": batch_all, "served_over_batch": served / batch_all,
             "one_at_a_time_s": t_seq, "one_at_a_time_path_steps_per_s": batch,
             "served_over_one_at_a_time": served / batch, "max_in_flight": stats["maxInFlight"],
             "peak_footprint_gb": stats["peakFootprint"] / 2**30}
+
+
+def grid_sweep(eng, stream, flush, npath):
+    """The precision workload's grid sweep: the same barrier risk on the 20x10, 60x30 and 120x60
+    surfaces, FP32 path form and FP64 form (CUDA events on the engine's stream, L2 flushed
+    between launches), and the FP32-FP64 difference of every risk in Monte Carlo standard
+    errors (from 8 independent FP32 seed pairs at a quarter of the paths)."""
+    import torch
+    from compfinance_gb300 import NumericalParam
+    u = W.UOC_BARRIER
+    out = {}
+    for g in ((20, 10), (60, 30), (120, 60)):
+        s, t, v = W.dupire_surface(*g)
+        mid = f"sweep{g[0]}x{g[1]}"
+        eng.putDupire(W.DUPIRE_SPOT, s, t, v, W.DUPIRE_MAXDT, mid)
+        npay, npar, dim = eng.shapes(mid, "uoc")
+        res = {}
+        risks = {}
+        for prec, reps in (("fp32", 3), ("fp64", 2)):
+            num = NumericalParam(numPath=npath, precision=prec)
+            eng.enqueue(mid, "uoc", num, risk=True)
+            torch.cuda.synchronize()
+            ms = []
+            for k in range(reps):
+                flush.fill_(float(k))
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                eng.enqueue(mid, "uoc", num, risk=True)
+                b.record(stream)
+                torch.cuda.synchronize()
+                ms.append(a.elapsed_time(b))
+            risks[prec] = eng.fetch(npay, npar)
+            best = min(ms)
+            res[prec] = {"ms_per_step": best, "paths_per_s": npath / (best / 1e3),
+                         "path_steps_per_s": npath * dim / (best / 1e3)}
+        se = []
+        for k in range(8):
+            eng.enqueue(mid, "uoc", NumericalParam(numPath=npath // 4, precision="fp32", seed1=1000 + k,
+                                                   seed2=77 + k), risk=True)
+            se.append(eng.fetch(npay, npar)[3])
+        se = np.std(np.array(se), axis=0, ddof=1) / 2.0
+        r32, r64 = risks["fp32"][3], risks["fp64"][3]
+        mask = se > 1e-3 * np.abs(r64).max()
+        res["fp32_over_fp64"] = res["fp64"]["ms_per_step"] / res["fp32"]["ms_per_step"]
+        res["max_risk_fp32_minus_fp64_in_stderr"] = float(np.max(np.abs(r32 - r64)[mask] / se[mask]))
+        res["price_fp32_minus_fp64_in_stderr"] = float(abs(risks["fp32"][0][0] - risks["fp64"][0][0]) /
+                                                       risks["fp64"][1][0])
+        out[f"{g[0]}x{g[1]}"] = res
+    return out
+
+
+def superbucket_leg(eng, npath=1 << 20):
+    """The superbucket workload: implied-vol surface (30 strikes x 12 maturities) calibrated to a
+    60x30 local-vol grid in FP64; 200 Europeans (10 maturities x 20 strikes), 36 monthly steps,
+    Sobol paths.  Times AADriskMulti (200 risk vectors of 1801 parameters) on the calibrated
+    model and the whole dupireSuperbucket chain (calibration, MC adjoints, calibration adjoint
+    to the 360 implied vols), in both precisions of the path arithmetic (wall clock, each call
+    synchronous)."""
+    from compfinance_gb300 import Engine, NumericalParam
+    iv = Engine.ivs("param", 100.0, [W.SB_IVS["a"], W.SB_IVS["b"], W.SB_IVS["c"], W.SB_IVS["sref"]])
+    isp, mds, itm, mdt = W.superbucket_grid(60, 30)
+    rk, rm = W.superbucket_riskview(30, 12)
+    mats, strikes = W.superbucket_portfolio(10, 20)
+    eng.putEuropeans(mats, strikes, "c4port")
+    cal = eng.dupireCalib(iv, isp, mds, itm, mdt)
+    eng.putDupire(100.0, cal["spots"], cal["times"], cal["lVols"], 1.0 / 12.0, "c4dup")
+    w = np.ones(len(mats))
+    out = {"paths": npath, "payoffs": len(mats), "params": 1 + len(cal["spots"]) * len(cal["times"]),
+           "implied_vols": len(rk) * len(rm)}
+    for prec in ("fp32", "fp64"):
+        num = NumericalParam(useSobol=True, numPath=npath, precision=prec)
+        eng.AADriskMulti("c4dup", "c4port", num)  # warm-up (plan lowering, buffers)
+        t0 = time.perf_counter()
+        eng.AADriskMulti("c4dup", "c4port", num)
+        t_multi = time.perf_counter() - t0
+        eng.dupireSuperbucket(iv, 100.0, 1.0 / 12.0, "c4port", w, isp, mds, itm, mdt, rk, rm, num)
+        t0 = time.perf_counter()
+        sb = eng.dupireSuperbucket(iv, 100.0, 1.0 / 12.0, "c4port", w, isp, mds, itm, mdt, rk, rm, num)
+        t_sb = time.perf_counter() - t0
+        out[prec] = {"aad_risk_multi_s": t_multi, "aad_risk_multi_paths_per_s": npath / t_multi,
+                     "superbucket_s": t_sb, "superbucket_value": sb["value"], "superbucket_delta": sb["delta"]}
+    return out
 
 
 def run_reference(args):
@@ -197,6 +284,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-stream leg")
+    ap.add_argument("--no-sweep", action="store_true", help="skip the grid sweep and superbucket legs")
     ap.add_argument("--serve-requests", type=int, default=10000)
     ap.add_argument("--paths", type=int, default=NPATH,
                     help="paths per step (default 2^22; smaller cases are for profiler captures only)")
@@ -321,6 +409,9 @@ def main():
         "clocks": clocks,
         "step_ms": [round(x, 4) for x in ms32],
     }
+    if not args.no_sweep:
+        out["grid_sweep"] = grid_sweep(eng, stream, flush, npath)
+        out["superbucket"] = superbucket_leg(eng)
     if not args.no_serving:
         out["serving"] = serving_leg(eng, args.serve_requests, seed=2026 + rank)
     if rank == 0 and not args.no_cpu:

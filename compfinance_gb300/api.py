@@ -192,6 +192,22 @@ class Engine:
         return dict(payoffIds=labels, payoffValues=v, riskPayoffValue=agg.value,
                     paramIds=self.parameterLabels(modelId), risks=r)
 
+    def modelGrid(self, modelId):
+        """(spots, times) of a Dupire model; raises for other models (cf_model_grid)."""
+        ns, nt = ctypes.c_int(), ctypes.c_int()
+        _check(lib().cf_model_grid(self._h, modelId.encode(), ctypes.byref(ns), ctypes.byref(nt), None, None))
+        spots, times = np.zeros(ns.value), np.zeros(nt.value)
+        _check(lib().cf_model_grid(self._h, modelId.encode(), ctypes.byref(ns), ctypes.byref(nt), _p(spots),
+                                   _p(times)))
+        return spots, times
+
+    def dupireAADRisk(self, modelId, productId, notionals, num):
+        """main.h:364-411: value, delta and the vega matrix [spots][times] of the aggregate."""
+        spots, times = self.modelGrid(modelId)
+        r = self.AADriskAggregate(modelId, productId, notionals, num)
+        return dict(value=r["riskPayoffValue"], delta=r["risks"][0],
+                    vega=np.asarray(r["risks"][1:]).reshape(len(spots), len(times)))
+
     def AADriskMulti(self, modelId, productId, num):
         npay, npar, _ = self.shapes(modelId, productId)
         v, r = np.zeros(npay), np.zeros(npar * npay)

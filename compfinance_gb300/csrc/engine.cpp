@@ -936,6 +936,20 @@ int cf_shapes(cf_context* ctx, const char* modelId, const char* productId, int* 
     return CF_OK;
 }
 
+int cf_model_grid(cf_context* ctx, const char* modelId, int* nSpots, int* nTimes, double* spots, double* times)
+{
+    CF_CTX();
+    auto it = ctx->c.models.find(modelId ? modelId : "");
+    if (it == ctx->c.models.end()) return fail(CF_E_NOTFOUND, "dupireAADRisk() : Model not found");
+    const ModelDesc& m = it->second;
+    if (m.kind != MODEL_DUPIRE) return fail(CF_E_ARG, "dupireAADRisk() : Model not a Dupire");
+    if (nSpots) *nSpots = int(m.spots.size());
+    if (nTimes) *nTimes = int(m.times.size());
+    if (spots) std::copy(m.spots.begin(), m.spots.end(), spots);
+    if (times) std::copy(m.times.begin(), m.times.end(), times);
+    return CF_OK;
+}
+
 int cf_value(cf_context* ctx, const char* modelId, const char* productId, const cf_num_param* num, double* values,
              double* stderrs)
 {

@@ -88,6 +88,10 @@ int cf_parameter_labels(cf_context* ctx, const char* modelId, char* buf, size_t 
 /* Sizes: number of payoffs, of model parameters, Gaussians per path (Model::simDim). */
 int cf_shapes(cf_context* ctx, const char* modelId, const char* productId, int* nPay, int* nParam,
               int* simDim);
+/* The local-vol grid of a Dupire model (Dupire::spots / times, mcMdlDupire.h:148-160): sizes,
+ * and the knots when spots / times are not NULL.  CF_E_NOTFOUND when the model is not in the
+ * store, CF_E_ARG when it is not a Dupire model (the checks of dupireAADRisk, main.h:371-383). */
+int cf_model_grid(cf_context* ctx, const char* modelId, int* nSpots, int* nTimes, double* spots, double* times);
 
 /* ---- entry points (main.h) --------------------------------------------------------- */
 /* value, main.h:43-96: path averages of every payoff; stderrs (optional) are the Monte

@@ -250,6 +250,29 @@ inline RiskResults AADriskAggregate(const std::string& modelId, const std::strin
     return r;
 }
 
+// dupireAADRisk, main.h:364-411: AADriskAggregate of a Dupire model, split into the value,
+// delta (risk to spot) and the vega matrix [spots][times] of the local-vol risks.
+struct DupireRiskResults
+{
+    double value = 0;
+    double delta = 0;
+    matrix<double> vega;
+};
+
+inline DupireRiskResults dupireAADRisk(const std::string& modelId, const std::string& productId,
+                                       const std::map<std::string, double>& notionals, const NumericalParam& num)
+{
+    int nS = 0, nT = 0;
+    detail::check(cf_model_grid(detail::ctx(), modelId.c_str(), &nS, &nT, nullptr, nullptr), "dupireAADRisk()");
+    const RiskResults agg = AADriskAggregate(modelId, productId, notionals, num);
+    DupireRiskResults r;
+    r.value = agg.riskPayoffValue;
+    r.delta = agg.risks[0];
+    r.vega.resize(size_t(nS), size_t(nT));
+    std::copy(agg.risks.begin() + 1, agg.risks.end(), r.vega.begin());
+    return r;
+}
+
 // RiskReports, main.h:260-266
 struct RiskReports
 {

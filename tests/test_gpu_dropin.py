@@ -31,4 +31,11 @@ def test_cpp_dropin_program(tmp_path):
     assert out["label0"] == r["payoffIds"][0]
     assert out["risk_value"] == r["riskPayoffValue"]
     assert out["risk0"] == r["risks"][0] and out["risk5"] == r["risks"][5]
+    # dupireAADRisk (main.h:364-411): the aggregate's value, spot risk and local-vol risks as a
+    # [spots][times] matrix; a Black-Scholes model is refused like the reference refuses it
+    agg = eng.AADriskAggregate("d", "u", {r["payoffIds"][0]: 1.0}, NumericalParam(numPath=1 << 14))
+    assert out["dupire"] == [agg["riskPayoffValue"], agg["risks"][0], agg["risks"][1 + 3 * 10 + 4]]
+    assert out["vega_shape"] == [20, 10] and out["not_dupire"] == 1
+    dr = eng.dupireAADRisk("d", "u", {r["payoffIds"][0]: 1.0}, NumericalParam(numPath=1 << 14))
+    assert dr["vega"].shape == (20, 10) and dr["vega"][3, 4] == agg["risks"][1 + 3 * 10 + 4]
     eng.close()

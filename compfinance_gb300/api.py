@@ -208,6 +208,20 @@ class Engine:
         return dict(value=r["riskPayoffValue"], delta=r["risks"][0],
                     vega=np.asarray(r["risks"][1:]).reshape(len(spots), len(times)))
 
+    BUMP_METHODS = {"auto": 0, "reprice": 1, "pathwise": 2}
+
+    def bumpRisk(self, modelId, productId, num, method="auto"):
+        """main.h:316-359: risks[nParam][nPay] by one-sided 1e-8 bumps, repriced on the same
+        random numbers in FP64 ('reprice' revalues each bumped model; 'pathwise' re-simulates
+        only the paths each bumped local-vol node touches)."""
+        npay, npar, _ = self.shapes(modelId, productId)
+        v, r = np.zeros(npay), np.zeros(npar * npay)
+        nc = num.c()
+        _check(lib().cf_bump_risk(self._h, modelId.encode(), productId.encode(), ctypes.byref(nc),
+                                  int(self.BUMP_METHODS[method]), _p(v), _p(r)))
+        return dict(payoffs=self.payoffLabels(productId), params=self.parameterLabels(modelId), values=v,
+                    risks=r.reshape(npar, npay))
+
     def AADriskMulti(self, modelId, productId, num):
         npay, npar, _ = self.shapes(modelId, productId)
         v, r = np.zeros(npay), np.zeros(npar * npay)

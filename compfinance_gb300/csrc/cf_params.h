@@ -136,6 +136,13 @@ struct McParams
     int nodeShiftF;
     long long nodeSlabOffset;
     const float* invnF;   // [512][4] piecewise-cubic inverse normal of the launch's generator
+
+    // Dupire raw inputs for bumped revaluation (bumpRisk): vols [nS][nT] spot-major, and per
+    // step sqrt(dt) and the time weight t of interp_lin, so that a bumped node's sqrt(dt) sigma
+    // is recomputed exactly like the host computes Y
+    const double* volsD;
+    const double* stepSqD;
+    const double* stepTwD;
 };
 
 // Kernel configuration chosen by the host.

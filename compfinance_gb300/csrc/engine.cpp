@@ -236,7 +236,7 @@ int Context::buildPlan(const ModelDesc& m, const ProductDesc& pd, Plan& plan)
     std::vector<double> ev(7 * size_t(plan.nEv), 0.0);
     double frontSpot = m.spot;
     size_t oBs = 0, oX = 0, oInv = 0, oY = 0, oXf = 0, oInvf = 0, oYf = 0, oCA = 0, oCB = 0, oCAf = 0, oCBf = 0,
-           oColA = 0, oColB = 0, oBsF = 0, oBucket = 0, oWA = 0, oWB = 0, oXs = 0, oIr = 0, oTd = 0, oBf = 0;
+           oColA = 0, oColB = 0, oBsF = 0, oBucket = 0, oWA = 0, oWB = 0, oXs = 0, oIr = 0, oTd = 0, oBf = 0, oVols = 0, oSq = 0, oTw = 0;
 
     if (m.kind == MODEL_BS)
     {
@@ -289,7 +289,7 @@ int Context::buildPlan(const ModelDesc& m, const ProductDesc& pd, Plan& plan)
             if (std::binary_search(pd.timeline.begin(), pd.timeline.end(), tl[i])) evAtStep[i] = e++;
         if (e != plan.nEv) return fail(CF_E_SHAPE, "Dupire: product dates before today are not supported");
         const int nS = int(m.spots.size()), nT = int(m.times.size());
-        std::vector<double> X(nS), inv(nS, 0.0), Y(size_t(n) * nS), cAv(n), cBv(n);
+        std::vector<double> X(nS), inv(nS, 0.0), Y(size_t(n) * nS), cAv(n), cBv(n), sqv(n), twv(n, 0.0);
         std::vector<int> colA(n), colB(n);
         for (int j = 0; j < nS; ++j) X[j] = std::log(m.spots[j]);
         for (int j = 0; j + 1 < nS; ++j) inv[j] = 1.0 / (X[j + 1] - X[j]);
@@ -297,6 +297,7 @@ int Context::buildPlan(const ModelDesc& m, const ProductDesc& pd, Plan& plan)
         for (int i = 0; i < n; ++i)
         {
             const double sq = std::sqrt(tl[i + 1] - tl[i]);
+            sqv[i] = sq;
             for (int j = 0; j < nS; ++j)
                 Y[size_t(i) * nS + j] = sq * interp_lin(m.times.data(), nT, &m.vols[size_t(j) * nT], tl[i]);
             const double* it = std::upper_bound(m.times.data(), m.times.data() + nT, tl[i]);
@@ -310,6 +311,7 @@ int Context::buildPlan(const ModelDesc& m, const ProductDesc& pd, Plan& plan)
             {
                 const int k = int(it - m.times.data()) - 1;
                 const double t = (tl[i] - m.times[k]) / (m.times[k + 1] - m.times[k]);
+                twv[i] = t;
                 colA[i] = k;
                 colB[i] = k + 1;
                 cAv[i] = sq * (1.0 - t);
@@ -364,6 +366,9 @@ int Context::buildPlan(const ModelDesc& m, const ProductDesc& pd, Plan& plan)
         P.nodeDirect = sMax >= 2048 ? 1 : 0;
         oWA = pk.vec(wA);
         oWB = pk.vec(wB);
+        oVols = pk.vec(m.vols);
+        oSq = pk.vec(sqv);
+        oTw = pk.vec(twv);
         // FP32 risk kernel (dupire_risk32): knots with sentinels, (xr, ir) per interval,
         // (y, d) per step and interval, and buckets narrower than 2/3 of the smallest knot
         // spacing.  Products whose dates are not monitoring dates plus a final maturity, grids
@@ -485,6 +490,9 @@ int Context::buildPlan(const ModelDesc& m, const ProductDesc& pd, Plan& plan)
         P.irF = (const float*)D(oIr);
         P.tdF = (const float*)D(oTd);
         P.bucketF = (const int*)D(oBf);
+        P.volsD = (const double*)D(oVols);
+        P.stepSqD = (const double*)D(oSq);
+        P.stepTwD = (const double*)D(oTw);
     }
     P.evAtStep = (const int*)D(oEv);
     P.evD = (const double*)D(oEvD);

@@ -114,6 +114,16 @@ int cf_aad_risk_aggregate(cf_context* ctx, const char* modelId, const char* prod
 int cf_aad_risk_multi(cf_context* ctx, const char* modelId, const char* productId, const cf_num_param* num,
                       double* values, double* risks);
 
+/* bumpRisk, main.h:316-359: values[nPay] and risks[nParam * nPay] (parameter-major, like
+ * AADriskMulti) by one-sided 1e-8 bumps of every model parameter, repriced on the same random
+ * numbers, always in FP64.  method: CF_BUMP_REPRICE revalues a bumped copy of the model per
+ * parameter (the reference's procedure); CF_BUMP_PATHWISE (Dupire) re-simulates, for each
+ * local-vol node, only the paths that touch it (the same numbers, far less work); CF_BUMP_AUTO
+ * picks pathwise where it applies. */
+enum { CF_BUMP_AUTO = 0, CF_BUMP_REPRICE = 1, CF_BUMP_PATHWISE = 2 };
+int cf_bump_risk(cf_context* ctx, const char* modelId, const char* productId, const cf_num_param* num, int method,
+                 double* values, double* risks);
+
 /* Implied-vol surfaces for the Dupire calibration (ivs.h): kind 0 =
  * iv(K,T) = p0 + p1 ln^2(K/p3)/sqrt(T) + p2 ln(K/p3); kind 1 = MertonIVS (ivs.h:147-179)
  * with p = {vol, jump intensity, mean jump, jump std}. */

@@ -297,6 +297,23 @@ inline RiskReports AADriskMulti(const std::string& modelId, const std::string& p
     return r;
 }
 
+// bumpRisk, main.h:316-359: one-sided 1e-8 bumps of every parameter, repriced on the same
+// random numbers (FP64), in the RiskReports layout.
+inline RiskReports bumpRisk(const std::string& modelId, const std::string& productId, const NumericalParam& num)
+{
+    const auto s = detail::shapes(modelId, productId, "bumpRisk() : Could not retrieve model and product");
+    RiskReports r;
+    r.values.resize(s.nPay);
+    r.risks.resize(size_t(s.nParam), size_t(s.nPay));
+    const cf_num_param n = detail::cnum(num);
+    detail::check(cf_bump_risk(detail::ctx(), modelId.c_str(), productId.c_str(), &n, CF_BUMP_AUTO, r.values.data(),
+                               &*r.risks.begin()),
+                  "bumpRisk()");
+    r.payoffs = getPayoffLabels(productId);
+    r.params = getParameterLabels(modelId);
+    return r;
+}
+
 struct CalibResults
 {
     std::vector<double> spots, times;

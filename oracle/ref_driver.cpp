@@ -387,6 +387,21 @@ int main()
             put("risk_value", {r.riskPayoffValue});
             put("risks", r.risks);
         }
+        else if (cmd == "bump")  // mid pid num : bumpRisk (main.h:316-359), one-sided 1e-8 bumps
+        {
+            string mid, pid;
+            std::cin >> mid >> pid;
+            auto num = rdnum(std::cin);
+            if (num.parallel) ensurePool();
+            double t0 = now_s();
+            auto r = bumpRisk(mid, pid, num);
+            double t1 = now_s();
+            put("values", r.values);
+            put("risks", std::vector<double>(r.risks.begin(),
+                r.risks.begin() + r.risks.rows() * r.risks.cols()));
+            put("shape", {double(r.risks.rows()), double(r.risks.cols())});
+            put("seconds", {t1 - t0});
+        }
         else if (cmd == "riskmulti")  // mid pid num
         {
             string mid, pid;

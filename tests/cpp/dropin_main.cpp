@@ -50,6 +50,7 @@ int main()
         threw = true;
     }
     const auto dr = dupireAADRisk("dupire", "uoc", {{v.identifiers[0], 1.0}}, num);
+    const auto br = bumpRisk("dupire", "uoc", num);
     bool notDupire = false;
     try
     {
@@ -62,10 +63,11 @@ int main()
     std::printf("{\"value\": [%.17g, %.17g], \"risk_value\": %.17g, \"risk0\": %.17g, \"risk5\": %.17g,"
                 " \"nparams\": %zu, \"bs\": [%.17g, %.17g, %.17g, %.17g, %.17g], \"multi_shape\": [%zu, %zu],"
                 " \"multi00\": %.17g, \"label0\": \"%s\", \"threw\": %d, \"dupire\": [%.17g, %.17g, %.17g],"
-                " \"vega_shape\": [%zu, %zu], \"not_dupire\": %d}\n",
+                " \"vega_shape\": [%zu, %zu], \"not_dupire\": %d, \"bump_shape\": [%zu, %zu], \"bump50\": %.17g}\n",
                 v.values[0], v.values[1], r.riskPayoffValue, r.risks[0], r.risks[5], r.risks.size(),
                 bs.riskPayoffValue, bs.risks[0], bs.risks[1], bs.risks[2], bs.risks[3], multi.risks.rows(),
                 multi.risks.cols(), multi.risks[0][0], r.payoffIds[0].c_str(), threw ? 1 : 0, dr.value, dr.delta,
-                dr.vega[3][4], dr.vega.rows(), dr.vega.cols(), notDupire ? 1 : 0);
+                dr.vega[3][4], dr.vega.rows(), dr.vega.cols(), notDupire ? 1 : 0, br.risks.rows(), br.risks.cols(),
+                br.risks[50][0]);
     return 0;
 }

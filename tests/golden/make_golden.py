@@ -3,11 +3,12 @@
 
 The reference's C++ (compiled in this container by oracle/build_ref.py into
 oracle/_ref/ref_driver) is driven through its own entry points (value, AADriskOne,
-AADriskAggregate, AADriskMulti, dupireCalib, dupireSuperbucket, the RNG classes).
+AADriskAggregate, AADriskMulti, bumpRisk, dupireCalib, dupireSuperbucket, the RNG classes).
 Every case records its inputs next to its outputs, so the fixtures are self-contained:
 the tests never need the reference.
 
-    python3 tests/golden/make_golden.py            # rebuilds the driver when missing
+    python3 tests/golden/make_golden.py [rng host mc calib bump]   # all when none named;
+                                                                   # rebuilds the driver when missing
 """
 import json
 import os
@@ -275,6 +276,34 @@ def mc_cases(models, products):
     return out
 
 
+def bump_cases(models, products):
+    """bumpRisk (main.h:316-359): every model parameter bumped by 1e-8 and the product repriced on
+    the same random numbers; risks[nParam][nPay] = 1e8 (bumped - base)."""
+    cases = [
+        ("bs_european_mrg", "bs", "euro", 0, 4096),
+        ("bs_europeans_sobol", "bs_spotmeasure", "europeans", 1, 1024),
+        ("bs_uoc_mrg", "bs", "uoc", 0, 1024),
+        ("dup20x10_uoc_mrg", "dup20x10", "uoc", 0, 1024),
+        ("dup20x10_uoc_sobol", "dup20x10", "uoc", 1, 512),
+        ("dup20x10_european_settle_sobol", "dup20x10", "euro_settle", 1, 1024),
+        ("dup60x30_uoc_mrg", "dup60x30", "uoc", 0, 256),
+        ("dup60x30_monthly_europeans_sobol", "dup60x30_monthly", "europeans", 1, 256),
+    ]
+    cmds = [model_cmd(mid, m) for mid, m in models.items()] + \
+           [product_cmd(pid, p) for pid, p in products.items()]
+    cmds += [f"bump {mid} {pid} {num(sob, n)}" for (_, mid, pid, sob, n) in cases]
+    it = iter(run(cmds))
+    out = {"models": models, "products": products, "cases": []}
+    for (name, mid, pid, sob, n) in cases:
+        rec = dict(name=name, model=mid, product=pid, sobol=sob, npath=n, seed1=12345, seed2=1234)
+        rec["values"] = next(it)[1]
+        rec["risks"] = next(it)[1]
+        rec["shape"] = [int(x) for x in next(it)[1]]
+        next(it)
+        out["cases"].append(rec)
+    return out
+
+
 def calib_cases():
     out = {}
     incl_spots, maxds, incl_times, maxdtv = W.superbucket_grid(60, 30)
@@ -331,8 +360,13 @@ def calib_cases():
 
 def main():
     models, products = models_products()
-    for name, obj in [("rng", rng_cases()), ("host", host_cases(models, products)),
-                      ("mc", mc_cases(models, products)), ("calib", calib_cases())]:
+    only = set(sys.argv[1:])
+    for name, fn in [("rng", rng_cases), ("host", lambda: host_cases(models, products)),
+                     ("mc", lambda: mc_cases(models, products)), ("calib", calib_cases),
+                     ("bump", lambda: bump_cases(models, products))]:
+        if only and name not in only:
+            continue
+        obj = fn()
         path = os.path.join(HERE, f"{name}.json")
         with open(path, "w") as fh:
             json.dump(obj, fh, separators=(",", ":"))

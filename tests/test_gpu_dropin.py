@@ -38,4 +38,7 @@ def test_cpp_dropin_program(tmp_path):
     assert out["vega_shape"] == [20, 10] and out["not_dupire"] == 1
     dr = eng.dupireAADRisk("d", "u", {r["payoffIds"][0]: 1.0}, NumericalParam(numPath=1 << 14))
     assert dr["vega"].shape == (20, 10) and dr["vega"][3, 4] == agg["risks"][1 + 3 * 10 + 4]
+    # bumpRisk (main.h:316-359) in the RiskReports layout
+    br = eng.bumpRisk("d", "u", NumericalParam(numPath=1 << 14))
+    assert out["bump_shape"] == [201, 2] and out["bump50"] == br["risks"][50, 0]
     eng.close()

@@ -292,6 +292,32 @@ class Engine:
                     microbucket=micro.reshape(nS.value, nT.value))
 
     # ---- RNG access --------------------------------------------------------------------------
+    def dupireSuperbucketBump(self, ivs, spot, maxDt, productId, notionals, inclSpots, maxDs, inclTimes, maxDtVol,
+                              strikes, mats, num, vegaBump=0.0):
+        """main.h:575-696: value, delta (spot +1e-8) and vega[strike][mat] (each risk-view implied
+        vol +vegaBump, the reference's 1e-5 when 0, recalibrated and repriced), FP64 valuations on
+        the same random numbers."""
+        labels = self.payoffLabels(productId)
+        w = np.zeros(len(labels))
+        if isinstance(notionals, dict):
+            for lab, x in notionals.items():
+                if lab not in labels:
+                    raise CfError(-2, "dupireSuperbucketBump() : payoff not found")
+                w[labels.index(lab)] = x
+        else:
+            w[:] = notionals
+        a, b = _arr(inclSpots), _arr(inclTimes)
+        k, m = _arr(strikes), _arr(mats)
+        vega = np.zeros(len(k) * len(m))
+        val, dl = ctypes.c_double(), ctypes.c_double()
+        nc = num.c()
+        _check(lib().cf_dupire_superbucket_bump(self._h, ctypes.byref(ivs), ctypes.c_double(spot),
+                                                ctypes.c_double(maxDt), productId.encode(), _p(w), _p(a), len(a),
+                                                ctypes.c_double(maxDs), _p(b), len(b), ctypes.c_double(maxDtVol), _p(k),
+                                                len(k), _p(m), len(m), ctypes.byref(nc), ctypes.c_double(vegaBump),
+                                                ctypes.byref(val), ctypes.byref(dl), _p(vega)))
+        return dict(value=val.value, delta=dl.value, strikes=k, mats=m, vega=vega.reshape(len(k), len(m)))
+
     def sobolPoints(self, dim, firstPath, nPaths):
         out = np.zeros(nPaths * dim, dtype=np.uint32)
         _check(lib().cf_sobol_points(self._h, int(dim), ctypes.c_int64(firstPath), int(nPaths),

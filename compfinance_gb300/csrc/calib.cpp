@@ -243,4 +243,76 @@ int cf_dupire_superbucket(cf_context* ctx, const cf_ivs* ivs, double spot, doubl
     return CF_OK;
 }
 
+// dupireSuperbucketBump, main.h:575-696: the superbucket by bumping.  The base book value
+// of the calibrated model; delta by the spot bumped by 1e-8 on the same local vols; vega[i][j]
+// by each risk-view implied vol bumped by vegaBump (the reference's 1e-5 by default),
+// recalibrated and repriced.  All valuations
+// in FP64 on the same random numbers.
+int cf_dupire_superbucket_bump(cf_context* ctx, const cf_ivs* ivs, double spot, double maxDt, const char* productId,
+                               const double* notionals, const double* inclSpots, int nInclSpots, double maxDs,
+                               const double* inclTimes, int nInclTimes, double maxDtVol, const double* strikes,
+                               int nStrikes, const double* mats, int nMats, const cf_num_param* num, double vegaBump,
+                               double* value, double* delta, double* vega)
+{
+    const double h = vegaBump > 0.0 ? vegaBump : 1.0e-05;  // main.h:674
+    if (!ctx || !ivs || !productId || !notionals || !num || !value || !delta || !vega)
+        return fail(CF_E_ARG, "null argument");
+    if (nStrikes < 1 || nMats < 1 || !strikes || !mats) return fail(CF_E_ARG, "superbucket: empty risk view");
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    Context& c = ctx->c;
+    cudaSetDevice(c.device);
+    if (!c.products.count(productId)) return fail(CF_E_NOTFOUND, "dupireSuperbucketBump() : product not found");
+    cf_num_param n64 = *num;
+    n64.precision = CF_FP64;
+    const std::string mid = "\x01superbucketBump";
+    int rc = CF_OK;
+    // the book value sum_k notionals[k] value_k of a Dupire model on the given local vols
+    auto book = [&](const CalibRun& r, const std::vector<double>& lv, double s0, double& out) -> int {
+        ModelDesc m;
+        m.kind = MODEL_DUPIRE;
+        m.spot = s0;
+        m.spots = r.spots;
+        m.times = r.times;
+        m.vols = lv;
+        m.maxDt = maxDt;
+        m.version = ++c.versionCounter;
+        m.build();
+        c.models[mid] = std::move(m);
+        Plan* plan;
+        int e = c.getPlan(mid, productId, plan);
+        if (e) return e;
+        std::vector<double> v(plan->nPay);
+        if ((e = c.enqueue(*plan, n64, false, nullptr)) || (e = c.fetch(v.data(), nullptr, nullptr, nullptr))) return e;
+        out = 0.0;
+        for (int k = 0; k < plan->nPay; ++k) out += notionals[k] * v[k];  // inner_product in payoff order
+        return CF_OK;
+    };
+    CalibRun base;
+    std::vector<double> lv;
+    if ((rc = calibrate(c, *ivs, inclSpots, nInclSpots, maxDs, inclTimes, nInclTimes, maxDtVol, strikes, nStrikes,
+                        mats, nMats, base)) ||
+        (rc = fetch_lvols(c, base, lv)) || (rc = book(base, lv, spot, *value)))
+        return rc;
+    double up = 0.0;
+    if ((rc = book(base, lv, spot + 1.0e-08, up))) return rc;
+    *delta = (up - *value) * 1.0e+08;
+    std::vector<double> spreads(size_t(nStrikes) * nMats, 0.0);
+    for (int i = 0; i < nStrikes; ++i)
+        for (int j = 0; j < nMats; ++j)
+        {
+            spreads[size_t(i) * nMats + j] = h;
+            CalibRun r;
+            std::vector<double> lvb;
+            double b = 0.0;
+            if ((rc = calibrate(c, *ivs, inclSpots, nInclSpots, maxDs, inclTimes, nInclTimes, maxDtVol, strikes,
+                                nStrikes, mats, nMats, r, spreads.data())) ||
+                (rc = fetch_lvols(c, r, lvb)) || (rc = book(r, lvb, spot, b)))
+                return rc;
+            vega[size_t(i) * nMats + j] = (b - *value) / h;
+            spreads[size_t(i) * nMats + j] = 0.0;
+        }
+    c.models.erase(mid);
+    return CF_OK;
+}
+
 }  // extern "C"

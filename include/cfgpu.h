@@ -157,6 +157,15 @@ int cf_dupire_superbucket(cf_context* ctx, const cf_ivs* ivs, double spot, doubl
                           const double* inclTimes, int nInclTimes, double maxDtVol, const double* strikes,
                           int nStrikes, const double* mats, int nMats, const cf_num_param* num, int refSeeding,
                           double* value, double* delta, double* vega, double* microbucket);
+/* dupireSuperbucketBump, main.h:575-696: the same outputs by bumping: delta by the spot +1e-8
+ * on the same local vols, vega[nStrikes][nMats] by each risk-view implied vol +vegaBump (0: the
+ * reference's 1e-5), recalibrated and repriced (FP64 valuations on the same random numbers).
+ * The reference takes Merton parameters; any cf_ivs is accepted here. */
+int cf_dupire_superbucket_bump(cf_context* ctx, const cf_ivs* ivs, double spot, double maxDt, const char* productId,
+                               const double* notionals, const double* inclSpots, int nInclSpots, double maxDs,
+                               const double* inclTimes, int nInclTimes, double maxDtVol, const double* strikes,
+                               int nStrikes, const double* mats, int nMats, const cf_num_param* num, double vegaBump,
+                               double* value, double* delta, double* vega);
 
 /* AADriskAggregate without any device allocation.  No counterpart in the reference.
  * For callers that cannot let a library allocate device memory during a call (memory

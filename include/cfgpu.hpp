@@ -399,4 +399,38 @@ inline SuperbucketResults dupireSuperbucket(double spot, double maxDt, const std
                                 num);
 }
 
+// dupireSuperbucketBump, main.h:575-696 (Merton surface, the reference's signature): delta by
+// the spot +1e-8, vega by each risk-view implied vol +1e-5, recalibrated and repriced.
+inline SuperbucketResults dupireSuperbucketBump(double spot, double maxDt, const std::string& productId,
+                                                const std::map<std::string, double>& notionals,
+                                                const std::vector<double>& inclSpots, double maxDs,
+                                                const std::vector<double>& inclTimes, double maxDtVol,
+                                                const std::vector<double>& strikes, const std::vector<double>& mats,
+                                                double vol, double jmpIntens, double jmpAverage, double jmpStd,
+                                                const NumericalParam& num)
+{
+    const cf_ivs ivs{1, spot, {vol, jmpIntens, jmpAverage, jmpStd}};
+    const auto labels = getPayoffLabels(productId);
+    std::vector<double> w(labels.size(), 0.0);
+    for (const auto& kv : notionals)
+    {
+        size_t k = 0;
+        while (k < labels.size() && labels[k] != kv.first) ++k;
+        if (k == labels.size()) throw std::runtime_error("dupireSuperbucketBump() : payoff not found");
+        w[k] = kv.second;
+    }
+    SuperbucketResults r;
+    r.strikes = strikes;
+    r.mats = mats;
+    r.vega.resize(strikes.size(), mats.size());
+    const cf_num_param n = detail::cnum(num);
+    detail::check(cf_dupire_superbucket_bump(detail::ctx(), &ivs, spot, maxDt, productId.c_str(), w.data(),
+                                             inclSpots.data(), int(inclSpots.size()), maxDs, inclTimes.data(),
+                                             int(inclTimes.size()), maxDtVol, strikes.data(), int(strikes.size()),
+                                             mats.data(), int(mats.size()), &n, 0.0, &r.value, &r.delta,
+                                             r.vega.v.data()),
+                  "dupireSuperbucketBump()");
+    return r;
+}
+
 }  // namespace cfgpu

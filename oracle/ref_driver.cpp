@@ -417,7 +417,7 @@ int main()
             put("shape", {double(r.risks.rows()), double(r.risks.cols())});
             put("seconds", {t1 - t0});
         }
-        else if (cmd == "calib" || cmd == "superbucket")
+        else if (cmd == "calib" || cmd == "superbucket" || cmd == "superbucket_bump")
         {
             // ivs: "param spot a b c sref" or "merton spot vol intens avejmp stdjmp"
             string kind;
@@ -471,7 +471,16 @@ int main()
             auto num = rdnum(std::cin);
             if (num.parallel) ensurePool();
             double t0 = now_s();
-            if (kind == "merton")
+            if (cmd == "superbucket_bump")  // merton only, as main.h:575-696
+            {
+                auto r = dupireSuperbucketBump(spot, maxDt, pid, nots, inclSpots, maxDs, inclTimes,
+                                               maxDtVol, strikes, mats, mv, mi, ma, ms, num);
+                put("sb_value", {r.value});
+                put("sb_delta", {r.delta});
+                put("sb_vega", std::vector<double>(r.vega.begin(),
+                    r.vega.begin() + r.vega.rows() * r.vega.cols()));
+            }
+            else if (kind == "merton")
             {
                 auto r = dupireSuperbucket(spot, maxDt, pid, nots, inclSpots, maxDs, inclTimes,
                                            maxDtVol, strikes, mats, mv, mi, ma, ms, num);

@@ -301,6 +301,28 @@ def bump_cases(models, products):
         rec["shape"] = [int(x) for x in next(it)[1]]
         next(it)
         out["cases"].append(rec)
+    # dupireSuperbucketBump (main.h:575-696): Merton surface, a reduced portfolio and risk view
+    mats, strikes = [], []
+    for t in (0.5, 1.0, 2.0):
+        for k in (90.0, 100.0, 115.0):
+            mats.append(t)
+            strikes.append(k)
+    small_s = [60.0, 80.0, 90.0, 100.0, 110.0, 125.0, 150.0]
+    small_t = [0.25, 0.5, 1.0, 2.0]
+    rv_k, rv_m = W.superbucket_riskview(8, 5)
+    nots = [(0, 1.0), (1, 2.0), (4, -1.0), (8, 0.5)]
+    mert = [0.15, 0.5, -0.1, 0.15]
+    ivs = "merton " + " ".join(f(x) for x in [100.0] + mert)
+    r = run([cmd_europeans("sbp", mats, strikes),
+             f"superbucket_bump {ivs} {len(small_s)} {fl(small_s)} {f(10.0)} {len(small_t)} {fl(small_t)} {f(0.25)} "
+             f"{f(1.0 / 12.0)} sbp {len(nots)} " + " ".join(f"{k} {f(w)}" for k, w in nots) +
+             f" {len(rv_k)} {fl(rv_k)} {len(rv_m)} {fl(rv_m)} {num(1, 1024)}"])
+    d = {tag: v for tag, v in r}
+    out["superbucket_bump"] = dict(ivs="merton", ivs_params=[100.0] + mert, incl_spots=small_s, max_ds=10.0,
+                                   incl_times=small_t, max_dt_vol=0.25, maxdt=1.0 / 12.0,
+                                   portfolio=dict(mats=mats, strikes=strikes), notionals=nots, rv_strikes=rv_k,
+                                   rv_mats=rv_m, sobol=1, npath=1024, value=d["sb_value"][0], delta=d["sb_delta"][0],
+                                   vega=d["sb_vega"])
     return out
 
 

@@ -246,6 +246,26 @@ def superbucket_leg(eng, npath=1 << 20):
     return out
 
 
+def bump_leg(eng):
+    """bumpRisk (finite differences, 1e-8 bumps of the 1801 parameters, FP64) of the C2 workload
+    (60x30 barrier, 156 weekly steps, mrg32k3a): the pathwise procedure at 2^16 and 2^18 paths and
+    full repricing at 2^16 (wall clock, synchronous calls), and their agreement."""
+    from compfinance_gb300 import NumericalParam
+    s, t, v = W.dupire_surface(60, 30)
+    eng.putDupire(W.DUPIRE_SPOT, s, t, v, W.DUPIRE_MAXDT, "bumpdup")
+    out = {"params": eng.shapes("bumpdup", "uoc")[1]}
+    eng.bumpRisk("bumpdup", "uoc", NumericalParam(numPath=1 << 12), method="pathwise")  # warm-up
+    res = {}
+    for n, method in ((1 << 16, "pathwise"), (1 << 18, "pathwise"), (1 << 16, "reprice")):
+        t0 = time.perf_counter()
+        res[(n, method)] = eng.bumpRisk("bumpdup", "uoc", NumericalParam(numPath=n), method=method)["risks"]
+        out[f"{method}_2^{n.bit_length() - 1}_s"] = time.perf_counter() - t0
+    a, b = res[(1 << 16, "pathwise")], res[(1 << 16, "reprice")]
+    out["pathwise_speedup_over_reprice_2^16"] = out["reprice_2^16_s"] / out["pathwise_2^16_s"]
+    out["pathwise_minus_reprice_rel_to_max_2^16"] = float(np.abs(a - b).max() / np.abs(b).max())
+    return out
+
+
 def run_reference(args):
     """The reference arm: the CPU restatement of the reference's path (the reference's own
     sources are not on the GPU host) on all host threads, W untimed + K timed steps, each step
@@ -412,6 +432,7 @@ def main():
     if not args.no_sweep:
         out["grid_sweep"] = grid_sweep(eng, stream, flush, npath)
         out["superbucket"] = superbucket_leg(eng)
+        out["bump_risk"] = bump_leg(eng)
     if not args.no_serving:
         out["serving"] = serving_leg(eng, args.serve_requests, seed=2026 + rank)
     if rank == 0 and not args.no_cpu:

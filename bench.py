@@ -334,15 +334,22 @@ def main():
     eng.putDupire(W.DUPIRE_SPOT, s, t, v, W.DUPIRE_MAXDT, "dupire")
     eng.putBarrier(u["strike"], u["barrier"], u["maturity"], u["monitor_freq"], u["smooth"], 0, "uoc")
     npay, npar, dim = eng.shapes("dupire", "uoc")
-    # Each rank simulates its own 2^22 paths (independent seeds): weak scaling, no exchange.
-    seed1 = W.MRG_SEEDS[0] + 7919 * rank
-    num32 = NumericalParam(numPath=npath, precision="fp32", seed1=seed1)
-    num64 = NumericalParam(numPath=npath, precision="fp64", seed1=seed1)
+    # With N ranks the step is one run of N x npath paths sharded by path range: rank r
+    # simulates paths [r npath, (r + 1) npath) (weak scaling), and the exact int64 accumulators
+    # are summed across ranks once, after the timed steps (compfinance_gb300/shard.py).
+    num32 = NumericalParam(numPath=npath, precision="fp32")
+    num64 = NumericalParam(numPath=npath, precision="fp64")
+    first = rank * npath
     flush = torch.empty(64 << 20, dtype=torch.float32, device="cuda")
+
+    def launch(num):
+        if world > 1:
+            return eng.enqueue_shard("dupire", "uoc", num, first, risk=True)
+        return eng.enqueue("dupire", "uoc", num, risk=True)
 
     def timed(num, steps, warmup):
         for _ in range(warmup):
-            eng.enqueue("dupire", "uoc", num, risk=True)
+            launch(num)
         torch.cuda.synchronize()
         if world > 1:
             torch.distributed.barrier()
@@ -353,7 +360,7 @@ def main():
         for k in range(steps):
             flush.fill_(float(k))
             evs[k][0].record(stream)
-            launches += eng.enqueue("dupire", "uoc", num, risk=True)
+            launches += launch(num)
             evs[k][1].record(stream)
         torch.cuda.synchronize()
         wall = time.perf_counter() - w0
@@ -369,6 +376,13 @@ def main():
     with Clocks(os.path.join(ROOT, "gpurun_out", f"bench_clocks_r{rank}.csv")) as ck:
         t32, ms32, launches, wall32 = timed(num32, args.steps, args.warmup)
     clocks = ck.summary()
+    sharded = None
+    if world > 1:
+        from compfinance_gb300.shard import combine
+        from compfinance_gb300.api import results_from_raw
+        tot = combine(eng.fetch_raw())
+        sv, se_, _, _ = results_from_raw(tot, npar, npay, world * npath)
+        sharded = {"paths": world * npath, "ranks": world, "price": float(sv[0]), "price_stderr": float(se_[0])}
     v32, e32, agg32, r32 = eng.fetch(npay, npar)
     steps64 = max(2, min(args.steps, 4))
     t64, ms64, _, _ = timed(num64, steps64, 1)
@@ -426,6 +440,7 @@ def main():
         "e2e": {"value": world * npath / e2e_t, "unit": "paths/s", "h2d_bytes_per_step": (h1 - h0) // ke,
                 "d2h_bytes_per_step": (d1 - d0) // ke},
         "gpu_launches": launches,
+        "sharded_run": sharded,
         "clocks": clocks,
         "step_ms": [round(x, 4) for x in ms32],
     }

@@ -345,11 +345,40 @@ class Engine:
                                 None if w is None else _p(w), ctypes.byref(n)))
         return n.value
 
+    def enqueue_shard(self, modelId, productId, num, firstPath, risk=True, weights=None):
+        """cf_enqueue_shard: paths [firstPath, firstPath + num.numPath) of the run's sequence."""
+        w = None if weights is None else _arr(weights)
+        n = ctypes.c_int()
+        nc = num.c()
+        _check(lib().cf_enqueue_shard(self._h, modelId.encode(), productId.encode(), ctypes.byref(nc),
+                                      ctypes.c_int64(int(firstPath)), int(bool(risk)), None if w is None else _p(w),
+                                      ctypes.byref(n)))
+        return n.value
+
+    def fetch_raw(self):
+        """The exact accumulators of the last enqueue (int64 words, hi/lo pairs)."""
+        nw = ctypes.c_int()
+        _check(lib().cf_fetch_raw(self._h, None, 0, ctypes.byref(nw)))
+        acc = np.zeros(nw.value, dtype=np.int64)
+        _check(lib().cf_fetch_raw(self._h, acc.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), nw.value,
+                                  ctypes.byref(nw)))
+        return acc
+
     def fetch(self, npay, nparam=0):
         v, e, r = np.zeros(npay), np.zeros(npay), np.zeros(max(nparam, 1))
         agg = ctypes.c_double()
         _check(lib().cf_fetch_result(self._h, _p(v), _p(e), ctypes.byref(agg), _p(r) if nparam else None))
         return v, e, agg.value, r[:nparam]
+
+
+def results_from_raw(acc, nRisk, nPay, nPath):
+    """cf_results_from_raw: (values, stderrs, aggregate, risks) of summed shard accumulators."""
+    acc = np.ascontiguousarray(acc, dtype=np.int64)
+    v, e, r = np.zeros(nPay), np.zeros(nPay), np.zeros(max(nRisk, 1))
+    agg = ctypes.c_double()
+    _check(lib().cf_results_from_raw(acc.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), int(nRisk), int(nPay),
+                                     ctypes.c_int64(int(nPath)), _p(v), _p(e), ctypes.byref(agg), _p(r)))
+    return v, e, agg.value, r[:nRisk]
 
 
 class CfRequest(ctypes.Structure):

@@ -43,8 +43,10 @@ constexpr int NODE_SHIFT = ROW_SHIFT + WEIGHT_SHIFT;
 //   nRisk+2nPay, +1              sum / sum of squares of the aggregate sum_k w_k payoff_k
 struct McParams
 {
-    // sizes
+    // sizes: the launch simulates paths [firstPath, firstPath + nPath) of the run's sequence
+    // (a shard; firstPath a multiple of 64, so antithetic pairs and Sobol warp batches stay whole)
     long long nPath;
+    long long firstPath;
     int nSteps;      // Gaussians per path (simDim)
     int nEv;         // product event dates
     int nPay;

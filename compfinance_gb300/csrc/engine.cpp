@@ -569,9 +569,11 @@ int Context::getPlan(const std::string& mid, const std::string& pid, Plan*& out)
 // weights upload, the accumulator reset, the kernel and the download of the accumulators
 // into the slot's pinned buffer are all asynchronous on the slot's stream; slot.done is
 // recorded after them.
-int Context::enqueue(Slot& slot, Plan& plan, const cf_num_param& num, bool risk, const double* weights)
+int Context::enqueue(Slot& slot, Plan& plan, const cf_num_param& num, bool risk, const double* weights,
+                     long long firstPath)
 {
     if (num.numPath <= 0) return fail(CF_E_ARG, "numPath must be positive");
+    if (firstPath < 0 || firstPath % 64) return fail(CF_E_ARG, "firstPath must be a non-negative multiple of 64");
     const bool sobol = num.useSobol != 0;
     if (sobol && !plan.sobolOk)
         return fail(CF_E_SHAPE, "Sobol dimension " + std::to_string(plan.nSteps) + " exceeds the " +
@@ -580,6 +582,7 @@ int Context::enqueue(Slot& slot, Plan& plan, const cf_num_param& num, bool risk,
     cudaStream_t st = slot.stream;
     McParams p = plan.base;
     p.nPath = num.numPath;
+    p.firstPath = firstPath;
     p.seed1 = unsigned(num.seed1);
     p.seed2 = unsigned(num.seed2);
     p.mrgJumpA = jumpA;
@@ -730,19 +733,27 @@ int Context::fetch(Slot& slot, double* values, double* stderrs, double* aggregat
     const long long* acc = static_cast<const long long*>(slot.hostAcc.ptr);
     const int e = *reinterpret_cast<const int*>(acc + 2 * size_t(p.nAcc));
     if (e) return fail(CF_E_DEVICE, "kernel error flag " + std::to_string(e));
-    const double n = double(p.nPath);
+    results_from_acc(acc, p.nRisk, p.nPay, p.nPath, values, stderrs, aggregate, slot.risk ? risks : nullptr);
+    return CF_OK;
+}
+
+// Path averages of the exact accumulators (hi, lo pairs): payoff means and Monte Carlo
+// standard errors, the aggregate's mean, the risks (parameter adjoints / nPath).
+void results_from_acc(const long long* acc, int nRisk, int nPay, long long nPath, double* values, double* stderrs,
+                      double* aggregate, double* risks)
+{
+    const double n = double(nPath);
     auto val = [&](int i) { return fix_value_host(acc[2 * size_t(i)], acc[2 * size_t(i) + 1]); };
-    for (int k = 0; k < p.nPay; ++k)
+    for (int k = 0; k < nPay; ++k)
     {
-        const double s = val(p.nRisk + k), q = val(p.nRisk + p.nPay + k);
+        const double s = val(nRisk + k), q = val(nRisk + nPay + k);
         const double mean = s / n;
         if (values) values[k] = mean;
         if (stderrs) stderrs[k] = std::sqrt(std::max(0.0, q / n - mean * mean) / n);
     }
-    if (aggregate) aggregate[0] = val(p.nRisk + 2 * p.nPay) / n;
-    if (risks && slot.risk)
-        for (int j = 0; j < p.nRisk; ++j) risks[j] = val(j) / n;
-    return CF_OK;
+    if (aggregate) aggregate[0] = val(nRisk + 2 * nPay) / n;
+    if (risks)
+        for (int j = 0; j < nRisk; ++j) risks[j] = val(j) / n;
 }
 
 double fix_value_host(long long hi, long long lo)
@@ -1047,6 +1058,54 @@ int cf_fetch_result(cf_context* ctx, double* values, double* stderrs, double* ag
 {
     CF_CTX();
     return ctx->c.fetch(values, stderrs, aggregate, risks);
+}
+
+int cf_enqueue_shard(cf_context* ctx, const char* modelId, const char* productId, const cf_num_param* num,
+                     int64_t firstPath, int risk, const double* weights, int* launches)
+{
+    CF_CTX();
+    if (!num) return fail(CF_E_ARG, "null argument");
+    Plan* plan;
+    int rc = ctx->c.getPlan(modelId ? modelId : "", productId ? productId : "", plan);
+    if (rc) return rc;
+    std::vector<double> w;
+    if (risk && !weights)
+    {
+        w.assign(plan->nPay, 0.0);
+        w[0] = 1.0;
+        weights = w.data();
+    }
+    ctx->c.main.stream = ctx->c.stream;
+    if ((rc = ctx->c.enqueue(ctx->c.main, *plan, *num, risk != 0, weights, (long long)firstPath))) return rc;
+    if (launches) *launches = ctx->c.main.launches;
+    return CF_OK;
+}
+
+int cf_fetch_raw(cf_context* ctx, int64_t* acc, int capacity, int* nWords)
+{
+    CF_CTX();
+    Slot& slot = ctx->c.main;
+    if (!slot.plan || slot.multi) return fail(CF_E_ARG, "no value or risk run enqueued");
+    CF_CUDA(cudaEventSynchronize(slot.done));
+    const McParams& p = slot.last;
+    const long long* h = static_cast<const long long*>(slot.hostAcc.ptr);
+    if (*reinterpret_cast<const int*>(h + 2 * size_t(p.nAcc))) return fail(CF_E_DEVICE, "kernel error flag");
+    if (nWords) *nWords = 2 * p.nAcc;
+    if (acc)
+    {
+        if (capacity < 2 * p.nAcc) return fail(CF_E_ARG, "accumulator buffer too small");
+        std::memcpy(acc, h, size_t(p.nAcc) * 16);
+    }
+    return CF_OK;
+}
+
+int cf_results_from_raw(const int64_t* acc, int nRisk, int nPay, int64_t nPath, double* values, double* stderrs,
+                        double* aggregate, double* risks)
+{
+    if (!acc || nRisk < 0 || nPay < 1 || nPath < 1) return fail(CF_E_ARG, "bad accumulators");
+    results_from_acc(reinterpret_cast<const long long*>(acc), nRisk, nPay, (long long)nPath, values, stderrs,
+                     aggregate, risks);
+    return CF_OK;
 }
 
 int cf_sobol_points(cf_context* ctx, int dim, int64_t firstPath, int nPaths, uint32_t* out)

@@ -16,6 +16,8 @@ namespace cf {
 int fail(int code, const std::string& msg);
 int cuda_fail(cudaError_t e, const char* what);
 double fix_value_host(long long hi, long long lo);
+void results_from_acc(const long long* acc, int nRisk, int nPay, long long nPath, double* values, double* stderrs,
+                      double* aggregate, double* risks);
 
 struct DevBuf
 {
@@ -131,7 +133,8 @@ struct Context
     int getPlan(const std::string& mid, const std::string& pid, Plan*& out);
     int buildPlan(const ModelDesc& m, const ProductDesc& pd, Plan& plan);
     const ProductDesc* productOf(const Plan& plan) const;
-    int enqueue(Slot& slot, Plan& plan, const cf_num_param& num, bool risk, const double* weights);
+    int enqueue(Slot& slot, Plan& plan, const cf_num_param& num, bool risk, const double* weights,
+                long long firstPath = 0);
     int fetch(Slot& slot, double* values, double* stderrs, double* aggregate, double* risks);
     bool ready(Slot& slot) const;
     size_t footprint(const Plan& plan, const cf_num_param& num, bool risk) const;

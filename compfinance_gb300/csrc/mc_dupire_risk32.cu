@@ -443,7 +443,7 @@ __global__ void __launch_bounds__(RB, 8) dupire_risk32(const McParams p)
         const long long u0 = tg * per;
         const long long u1 = u0 + per < nUnits ? u0 + per : nUnits;
         MrgState st{};
-        if (u0 < u1) st = mrg_jump(p.seed1, p.seed2, (unsigned long long)u0 * nSteps, p.mrgJumpA, p.mrgJumpB);
+        if (u0 < u1) st = mrg_jump(p.seed1, p.seed2, (unsigned long long)(p.firstPath / 2 + u0) * nSteps, p.mrgJumpA, p.mrgJumpB);
         for (long long it = 0; it < per; ++it)  // the same trip count for every thread of the grid
         {
             const long long u = u0 + it;
@@ -473,7 +473,7 @@ __global__ void __launch_bounds__(RB, 8) dupire_risk32(const McParams p)
             {
                 __syncwarp();
                 for (int d = lane; d < nSteps; d += 32)
-                    base[d] = sobol_state(p.sobolDir, nSteps, d, (unsigned long long)b * 32);
+                    base[d] = sobol_state(p.sobolDir, nSteps, d, (unsigned long long)(p.firstPath + b * 32));
                 __syncwarp();
                 const long long n = b * 32 + lane;
                 nAct = (n >= 1 && n <= p.nPath) ? 1 : 0;

@@ -569,7 +569,7 @@ __global__ void __launch_bounds__(MC_BLOCK) mc_kernel(const McParams p)
         const long long u0 = tg * per;
         const long long u1 = u0 + per < nUnits ? u0 + per : nUnits;
         MrgState st{};
-        if (u0 < u1) st = mrg_jump(p.seed1, p.seed2, (unsigned long long)u0 * nSteps, p.mrgJumpA, p.mrgJumpB);
+        if (u0 < u1) st = mrg_jump(p.seed1, p.seed2, (unsigned long long)(p.firstPath / 2 + u0) * nSteps, p.mrgJumpA, p.mrgJumpB);
         // uniform trip count across the block so that the node slab can be flushed in step
         for (long long it = 0; it < per; ++it)
         {
@@ -597,7 +597,7 @@ __global__ void __launch_bounds__(MC_BLOCK) mc_kernel(const McParams p)
             if (b >= nBatches) continue;
             __syncwarp();
             for (int d = lane; d < nSteps; d += 32)
-                base[d] = sobol_state(p.sobolDir, nSteps, d, (unsigned long long)b * 32);
+                base[d] = sobol_state(p.sobolDir, nSteps, d, (unsigned long long)(p.firstPath + b * 32));
             __syncwarp();
             const long long n = b * 32 + lane;
             const int nAct = (n >= 1 && n <= p.nPath) ? 1 : 0;

@@ -283,7 +283,7 @@ __global__ void __launch_bounds__(MC_BLOCK) multi_kernel(const MultiParams mp)
         const long long u1 = u0 + per < nUnits ? u0 + per : nUnits;
         if (u0 < u1)
         {
-            MrgState st = mrg_jump(p.seed1, p.seed2, (unsigned long long)u0 * nSteps, p.mrgJumpA, p.mrgJumpB);
+            MrgState st = mrg_jump(p.seed1, p.seed2, (unsigned long long)(p.firstPath / 2 + u0) * nSteps, p.mrgJumpA, p.mrgJumpB);
             for (long long u = u0; u < u1; ++u)
                 runUnit((2 * u + 1 < p.nPath) ? 2 : 1, [&](int) { return mrg_gauss<Real>(mrg_next(st)); });
         }
@@ -299,7 +299,7 @@ __global__ void __launch_bounds__(MC_BLOCK) multi_kernel(const MultiParams mp)
         {
             __syncwarp();
             for (int d = lane; d < nSteps; d += 32)
-                base[d] = sobol_state(p.sobolDir, nSteps, d, (unsigned long long)b * 32);
+                base[d] = sobol_state(p.sobolDir, nSteps, d, (unsigned long long)(p.firstPath + b * 32));
             __syncwarp();
             const long long n = b * 32 + lane;
             if (n >= 1 && n <= p.nPath)

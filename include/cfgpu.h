@@ -199,6 +199,25 @@ int cf_enqueue(cf_context* ctx, const char* modelId, const char* productId, cons
  * aggregate (optional), risks[nParam] (risk runs, optional). */
 int cf_fetch_result(cf_context* ctx, double* values, double* stderrs, double* aggregate, double* risks);
 
+/* ---- shards of one run (one per GPU, or per call) ------------------------------------ */
+/* The paths of a Monte Carlo run are independent, and every sum of a run is kept exactly in
+ * integer fixed point (pairs of int64: units of 2^-20 and 2^-60).  A run of N paths can
+ * therefore be cut into shards of contiguous path ranges, simulated anywhere, and summed
+ * exactly (the sharding of mcParallelSimul's path loop, mcBase.h:331-400, across devices):
+ *   cf_enqueue_shard   like cf_enqueue, for paths [firstPath, firstPath + num->numPath) of
+ *                      the run's random sequence (firstPath a multiple of 64);
+ *   cf_fetch_raw       the raw accumulators of the last enqueue (2 * (nParam + 2 nPay + 2)
+ *                      int64 words for a risk run, 2 * (2 nPay + 2) for a value run;
+ *                      *nWords receives the count);
+ *   cf_results_from_raw  values, stderrs, aggregate, risks of accumulators summed over the
+ *                      shards (word-wise int64 sums), for the run's total path count: bit-
+ *                      identical to one call over all the paths.  Needs no context. */
+int cf_enqueue_shard(cf_context* ctx, const char* modelId, const char* productId, const cf_num_param* num,
+                     int64_t firstPath, int risk, const double* weights, int* launches);
+int cf_fetch_raw(cf_context* ctx, int64_t* acc, int capacity, int* nWords);
+int cf_results_from_raw(const int64_t* acc, int nRisk, int nPay, int64_t nPath, double* values, double* stderrs,
+                        double* aggregate, double* risks);
+
 /* ---- serving loop (no counterpart in the reference: main.h runs one call at a time on the
  * ThreadPool, threadPool.h:30-172) -------------------------------------------------------- */
 typedef struct cf_server cf_server;

@@ -130,6 +130,11 @@ class Engine:
                                     int(bool(callPut)), id.encode()))
         return id
 
+    def putContingent(self, coupon, maturity, payFreq, smooth, id):
+        """store.h:165-180: the contingent bond of mcPrd.h:404-574."""
+        _check(lib().cf_put_contingent(self._h, ctypes.c_double(coupon), ctypes.c_double(maturity),
+                                       ctypes.c_double(payFreq), ctypes.c_double(smooth), id.encode()))
+
     def putEuropeans(self, maturities, strikes, id):
         m, k = _arr(maturities), _arr(strikes)
         _check(lib().cf_put_europeans(self._h, _p(m), _p(k), len(m), id.encode()))

@@ -9,7 +9,7 @@
 namespace cf {
 
 enum ModelKind : int { MODEL_BS = 0, MODEL_DUPIRE = 1 };
-enum ProductKind : int { PROD_EUROPEAN = 0, PROD_UOC = 1, PROD_EUROPEANS = 2 };
+enum ProductKind : int { PROD_EUROPEAN = 0, PROD_UOC = 1, PROD_EUROPEANS = 2, PROD_CONTINGENT = 3 };
 enum RngKind : int { RNG_MRG = 0, RNG_SOBOL = 1 };
 
 // Error bits written by kernels into McParams::err (host turns them into CF_E_DEVICE).
@@ -95,12 +95,15 @@ struct McParams
 
     // events
     const int* evAtStep;  // [nSteps+1] product date index reached at timeline point i, or -1
-    const double* evD;    // [7][nEv]: ff, tauF, disc, tauD, numeraire (factor), t, needNum
+    const int* evPoint;   // [nEv] timeline point of product date e
+    const double* evD;    // [10][nEv]: ff, tauF, disc, tauD, numeraire (factor), t, needNum,
+                          // libor(t_e, t_e+1), its derivative to the rate, coverage t_e+1 - t_e
     const float* evF;
 
     // product
     int callPut;
     double strike, barSmooth, minusSmooth, twoSmooth;
+    double coupon, cbSmooth;  // contingent bond: coupon, smoothing width (first spot x smooth)
     double logBandD;      // band test threshold in the state variable (FP64 form)
     float logBandF;       // (FP32 form)
     const double* kD;     // Europeans strikes, flattened by event

@@ -116,7 +116,30 @@ void ProductDesc::build()
     labels.clear();
     kflat.clear();
     payOff.clear();
-    if (kind == PROD_EUROPEAN)
+    libEnd.clear();
+    if (kind == PROD_CONTINGENT)
+    {
+        // mcPrd.h:426-480: today, every payFreq while more than a day remains, maturity
+        constexpr double kOneDay = 0.003773585;  // mcPrd.h:27
+        timeline.push_back(0.0);
+        double t = freq;
+        while (maturity - t > kOneDay)
+        {
+            timeline.push_back(t);
+            t += freq;
+        }
+        timeline.push_back(maturity);
+        const size_t n = timeline.size();
+        for (size_t i = 0; i < n; ++i)
+        {
+            fwdMat.push_back(timeline[i]);
+            discMat.push_back(NAN);
+            needNum.push_back(i > 0 ? 1 : 0);
+            libEnd.push_back(i + 1 < n ? timeline[i + 1] : NAN);
+        }
+        labels = {"contingent bond " + fmt2(maturity) + " " + fmt2(coupon)};
+    }
+    else if (kind == PROD_EUROPEAN)
     {
         timeline = {exercise};
         fwdMat = {settlement};
@@ -233,7 +256,7 @@ int Context::buildPlan(const ModelDesc& m, const ProductDesc& pd, Plan& plan)
     Packer pk;
     std::vector<double> tl;
     std::vector<int> evAtStep;
-    std::vector<double> ev(7 * size_t(plan.nEv), 0.0);
+    std::vector<double> ev(10 * size_t(plan.nEv), 0.0);
     double frontSpot = m.spot;
     size_t oBs = 0, oX = 0, oInv = 0, oY = 0, oXf = 0, oInvf = 0, oYf = 0, oCA = 0, oCB = 0, oCAf = 0, oCBf = 0,
            oColA = 0, oColB = 0, oBsF = 0, oBucket = 0, oWA = 0, oWB = 0, oXs = 0, oIr = 0, oTd = 0, oBf = 0, oVols = 0, oSq = 0, oTw = 0;
@@ -271,6 +294,12 @@ int Context::buildPlan(const ModelDesc& m, const ProductDesc& pd, Plan& plan)
             ev[4 * plan.nEv + e] = m.qSpot ? std::exp(m.div * t) / m.spot : std::exp(m.rate * t);
             ev[5 * plan.nEv + e] = t;
             ev[6 * plan.nEv + e] = pd.needNum[e] ? 1.0 : 0.0;
+            if (!pd.libEnd.empty() && !std::isnan(pd.libEnd[e]))  // mcMdlBS.h:266-272
+            {
+                const double dt = pd.libEnd[e] - t;
+                ev[7 * plan.nEv + e] = (std::exp(m.rate * dt) - 1.0) / dt;
+                ev[8 * plan.nEv + e] = std::exp(m.rate * dt);
+            }
         }
         frontSpot = m.spot * ev[0];  // path.front() forward of the first product date
         oBs = pk.vec(bsd);
@@ -447,6 +476,17 @@ int Context::buildPlan(const ModelDesc& m, const ProductDesc& pd, Plan& plan)
         P.logBandF = float(m.kind == MODEL_DUPIRE ? lb - P.x0d - 1e-5 : lb - 1e-5);
     }
 
+    if (pd.kind == PROD_CONTINGENT)
+    {
+        // coverages myDt (mcPrd.h:441-452); smoothing from the first spot (mcPrd.h:531-532)
+        for (int e = 0; e + 1 < plan.nEv; ++e) ev[9 * plan.nEv + e] = pd.timeline[e + 1] - pd.timeline[e];
+        P.coupon = pd.coupon;
+        P.cbSmooth = frontSpot * pd.smooth;
+    }
+    std::vector<int> evPoint(std::max(1, plan.nEv), 0);
+    for (int i = 0; i <= plan.nSteps; ++i)
+        if (evAtStep[i] >= 0) evPoint[evAtStep[i]] = i;
+    const size_t oEvPt = pk.vec(evPoint);
     const size_t oEv = pk.vec(evAtStep);
     const size_t oEvD = pk.vec(ev), oEvF = pk.vec(to_f(ev));
     std::vector<double> kf = pd.kflat;
@@ -495,6 +535,7 @@ int Context::buildPlan(const ModelDesc& m, const ProductDesc& pd, Plan& plan)
         P.stepTwD = (const double*)D(oTw);
     }
     P.evAtStep = (const int*)D(oEv);
+    P.evPoint = (const int*)D(oEvPt);
     P.evD = (const double*)D(oEvD);
     P.evF = (const float*)D(oEvF);
     P.kD = (const double*)D(oK);
@@ -870,6 +911,23 @@ int cf_put_european(cf_context* ctx, double strike, double exerciseDate, double 
     p.strike = strike;
     p.exercise = exerciseDate;
     p.settlement = settlementDate;
+    p.version = ++ctx->c.versionCounter;
+    p.build();
+    ctx->c.products[id] = std::move(p);
+    return CF_OK;
+}
+
+int cf_put_contingent(cf_context* ctx, double coupon, double maturity, double payFreq, double smooth, const char* id)
+{
+    CF_CTX();
+    if (check_id(id)) return CF_E_ARG;
+    if (!(payFreq > 0) || !(maturity > 0)) return fail(CF_E_ARG, "putContingent: bad maturity or frequency");
+    ProductDesc p;
+    p.kind = PROD_CONTINGENT;
+    p.coupon = coupon;
+    p.maturity = maturity;
+    p.freq = payFreq;
+    p.smooth = smooth <= 0 ? 0.0 : smooth;  // store.h:172
     p.version = ++ctx->c.versionCounter;
     p.build();
     ctx->c.products[id] = std::move(p);

@@ -50,10 +50,11 @@ struct ProductDesc
 {
     int kind = PROD_EUROPEAN;
     double strike = 0, exercise = 0, settlement = 0, barrier = 0, maturity = 0, freq = 0, smooth = 0;
+    double coupon = 0;  // contingent bond
     int callPut = 0;
     std::vector<double> mats, strikes;  // Europeans input pairs
     // derived
-    std::vector<double> timeline, fwdMat, discMat, kflat;
+    std::vector<double> timeline, fwdMat, discMat, kflat, libEnd;  // libEnd: libor end per date, NaN if none
     std::vector<int> needNum, payOff;
     std::vector<std::string> labels;
     unsigned long long version = 0;

@@ -13,6 +13,7 @@ const void* mc_kernel_ptr_bs_f64(int prod, int rng, int risk)
     CF_K3(PROD_EUROPEAN)
     CF_K3(PROD_UOC)
     CF_K3(PROD_EUROPEANS)
+    CF_K3(PROD_CONTINGENT)
 #undef CF_K3
 #undef CF_K2
 #undef CF_K

@@ -140,6 +140,7 @@ __global__ void __launch_bounds__(MC_BLOCK) mc_kernel(const McParams p)
     const Real sScale = F32 ? (Real)p.s0f : Real(1);
     const Real spot = (Real)p.spot;
     const Real w0 = nPay > 0 ? wts[0] : Real(0), w1 = nPay > 1 ? wts[1] : Real(0);
+    const Real cpn = (Real)p.coupon, cbSmooth = (Real)p.cbSmooth, cbTwo = Real(2) * (Real)p.cbSmooth;
 
     const long long T = (long long)gridDim.x * MC_BLOCK;
     const long long tg = (long long)blockIdx.x * MC_BLOCK + tid;
@@ -233,6 +234,7 @@ __global__ void __launch_bounds__(MC_BLOCK) mc_kernel(const McParams p)
     // ---------------------------------------------------------------------------------
     auto runUnit = [&](int nAct, auto&& gen) {
         Real x[NP], alive[NP], euro[NP], fE[NP], dE[NP], nE[NP], agg[NP];
+        Real cPrev[NP], cPay[NP];  // contingent bond: spot at the previous date, payoff so far
         bool dead[NP];
 #pragma unroll
         for (int a = 0; a < NP; ++a)
@@ -242,6 +244,7 @@ __global__ void __launch_bounds__(MC_BLOCK) mc_kernel(const McParams p)
             euro[a] = fE[a] = dE[a] = Real(0);
             nE[a] = Real(1);
             agg[a] = Real(0);
+            cPrev[a] = cPay[a] = Real(0);
             dead[a] = false;
         }
 
@@ -284,6 +287,20 @@ __global__ void __launch_bounds__(MC_BLOCK) mc_kernel(const McParams p)
                     const Real m = p.callPut ? (strike - F) : (F - strike);
                     euro[a] = (m > Real(0) ? m : Real(0)) / N;
                 }
+            }
+            else if (PROD == PROD_CONTINGENT)
+            {
+                // mcPrd.h:522-573: at the end of each period, (libor + coupon) x coverage when the
+                // spot rose (a digital smoothed over +-smooth), paid at the period's end; the
+                // redemption at maturity
+                if (e > 0)
+                {
+                    const Real dlt = F - cPrev[a];
+                    const Real dig = dlt > cbSmooth ? Real(1) : dlt < -cbSmooth ? Real(0) : (dlt + cbSmooth) / cbTwo;
+                    cPay[a] += dig * (ev[7 * nEv + e - 1] + cpn) * ev[9 * nEv + e - 1] / N;
+                }
+                cPrev[a] = F;
+                if (last) cPay[a] += Real(1) / N;
             }
             else
             {
@@ -361,6 +378,12 @@ __global__ void __launch_bounds__(MC_BLOCK) mc_kernel(const McParams p)
                 fix_add(&paySlab[2 * (sqBase + 1)], euro[a] * euro[a]);
                 agg[a] = w0 * p0 + w1 * euro[a];
             }
+            else if (PROD == PROD_CONTINGENT)
+            {
+                fix_add(&paySlab[2 * payBase], cPay[a]);
+                fix_add(&paySlab[2 * sqBase], cPay[a] * cPay[a]);
+                agg[a] = w0 * cPay[a];
+            }
             if (RISK)
             {
                 fix_add(&paySlab[2 * aggBase], agg[a]);
@@ -373,10 +396,12 @@ __global__ void __launch_bounds__(MC_BLOCK) mc_kernel(const McParams p)
         // Reverse sweep.
         // ---------------------------------------------------------------------------
         Real ax[NP], aAlive[NP], aEuro[NP], aVol[NP], aR[NP], aDv[NP], aSp[NP];
+        Real cAprev[NP];  // contingent bond: adjoint of the previous date's spot
 #pragma unroll
         for (int a = 0; a < NP; ++a)
         {
             ax[a] = aVol[a] = aR[a] = aDv[a] = aSp[a] = Real(0);
+            cAprev[a] = Real(0);
             aEuro[a] = dead[a] ? w1 : w0 * alive[a] + w1;       // payoff0 = alive*euro, payoff1 = euro
             aAlive[a] = dead[a] ? Real(0) : w0 * euro[a];
         }
@@ -431,6 +456,29 @@ __global__ void __launch_bounds__(MC_BLOCK) mc_kernel(const McParams p)
                             const Real before = SCR(F_AL + a, i);
                             aF += aAlive[a] * before * (Real(-1) / twoSmooth);
                             aAlive[a] *= (barSmooth - F) / twoSmooth;
+                        }
+                    }
+                    else if (PROD == PROD_CONTINGENT)
+                    {
+                        aF = cAprev[a];  // from the period that starts here
+                        cAprev[a] = Real(0);
+                        if (last) aN = -w0 / (N * N);
+                        if (e > 0)
+                        {
+                            // the period ending here: its start spot from the state at its date
+                            const Real xp = SCR(F_X + a, p.evPoint[e - 1]);
+                            const Real Fp = MODEL == MODEL_BS ? spotOf(xp) * ev[e - 1] : spotOf(xp);
+                            const Real dlt = F - Fp;
+                            const Real L = ev[7 * nEv + e - 1], cov = ev[9 * nEv + e - 1];
+                            const Real dig = dlt > cbSmooth ? Real(1) : dlt < -cbSmooth ? Real(0) : (dlt + cbSmooth) / cbTwo;
+                            if (!(dlt > cbSmooth) && !(dlt < -cbSmooth))
+                            {
+                                const Real aDl = w0 * (L + cpn) * cov / N / cbTwo;
+                                aF += aDl;
+                                cAprev[a] = -aDl;
+                            }
+                            aN -= w0 * dig * (L + cpn) * cov / (N * N);
+                            if (MODEL == MODEL_BS) aR[a] += w0 * dig * cov / N * ev[8 * nEv + e - 1];  // d libor / d r
                         }
                     }
                     else

@@ -72,6 +72,10 @@ int cf_put_dupire(cf_context* ctx, double spot, const double* spots, int nSpots,
 int cf_put_european(cf_context* ctx, double strike, double exerciseDate, double settlementDate,
                     const char* id);
 /* putBarrier, store.h:144-163 (smooth <= 0 is replaced by 1e-8 as in the reference) */
+/* putContingent, store.h:165-180 (ContingentBond, mcPrd.h:404-574): pays (libor(Ti, Ti+1) +
+ * coupon) x (Ti+1 - Ti) at Ti+1 when the spot rose over the period (a digital smoothed over
+ * +-smooth x the first spot; smooth <= 0: a sharp digital), plus the redemption at maturity. */
+int cf_put_contingent(cf_context* ctx, double coupon, double maturity, double payFreq, double smooth, const char* id);
 int cf_put_barrier(cf_context* ctx, double strike, double barrier, double maturity, double monitorFreq,
                    double smooth, int callPut, const char* id);
 /* putEuropeans, store.h:184-205 (maturities in increasing order) */

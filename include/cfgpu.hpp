@@ -160,6 +160,12 @@ inline void putBarrier(double strike, double barrier, double maturity, double mo
                   "putBarrier()");
 }
 
+// store.h:165-180
+inline void putContingent(double coupon, double maturity, double payFreq, double smooth, const std::string& store)
+{
+    detail::check(cf_put_contingent(detail::ctx(), coupon, maturity, payFreq, smooth, store.c_str()), "putContingent()");
+}
+
 inline void putEuropeans(const std::vector<double>& maturities, const std::vector<double>& strikes,
                          const std::string& store)
 {

@@ -26,7 +26,7 @@ class OrcProduct(ctypes.Structure):
     _fields_ = [("kind", ctypes.c_int), ("strike", ctypes.c_double), ("exercise", ctypes.c_double),
                 ("settlement", ctypes.c_double), ("barrier", ctypes.c_double), ("maturity", ctypes.c_double),
                 ("freq", ctypes.c_double), ("smooth", ctypes.c_double), ("callput", ctypes.c_int),
-                ("n", ctypes.c_int), ("mats", _dp), ("strikes", _dp)]
+                ("n", ctypes.c_int), ("mats", _dp), ("strikes", _dp), ("coupon", ctypes.c_double)]
 
 
 class OrcIvs(ctypes.Structure):
@@ -97,6 +97,9 @@ class Product:
             p.kind = 1
             p.strike, p.barrier, p.maturity = spec["strike"], spec["barrier"], spec["maturity"]
             p.freq, p.smooth, p.callput = spec["freq"], spec["smooth"], int(spec.get("callput", 0))
+        elif spec["kind"] == "contingent":
+            p.kind = 3
+            p.coupon, p.maturity, p.freq, p.smooth = spec["coupon"], spec["maturity"], spec["freq"], spec["smooth"]
         else:
             p.kind = 2
             m, pm = _arr(spec["mats"])

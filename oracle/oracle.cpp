@@ -23,6 +23,7 @@ using std::vector;
 constexpr double kEps = 1.0e-08;                  // gaussians.h:8, utility.h:9
 constexpr double kHalfDay = 0.00136986301369863;  // mcMdlDupire.h:26
 constexpr double kOneHour = 0.000114469;          // mcPrd.h:26, mcMdlDupire.h:333
+constexpr double kOneDay = 0.003773585;           // mcPrd.h:27
 constexpr double kOneOver2Pow32 = 2.3283064365387E-10;  // sobol.h:26 (truncated constant)
 
 // ---------------------------------------------------------------------------------------
@@ -416,7 +417,7 @@ struct Mrg : Rng
 template <class T>
 struct Sample
 {
-    T numeraire, forward, discount;
+    T numeraire, forward, discount, libor;
 };
 
 struct ProductDef
@@ -425,6 +426,7 @@ struct ProductDef
     vector<double> fwdMat;   // forward maturity per event (forwardMats[0][0])
     vector<double> discMat;  // discount maturity per event, NaN when none
     vector<int> needNum;
+    vector<double> libEnd;   // libor(t, libEnd) per event, NaN when none
     vector<std::string> labels;
 };
 
@@ -471,6 +473,28 @@ ProductDef productDef(const orc_product& p)
         d.labels = {l1 + " up and out " + fmt2(p.barrier) + " monitoring freq " + fmt2(p.freq) + " smooth " + fmt2(sm),
                     l1};
     }
+    else if (p.kind == 3)
+    {
+        // mcPrd.h:426-480: today, every payFreq while more than a day remains, maturity; spot
+        // on every date, libor(Ti, Ti+1) on every date but the last, numeraire after today
+        d.timeline.push_back(0.0);
+        double t = p.freq;
+        while (p.maturity - t > kOneDay)
+        {
+            d.timeline.push_back(t);
+            t += p.freq;
+        }
+        d.timeline.push_back(p.maturity);
+        const size_t n = d.timeline.size();
+        for (size_t i = 0; i < n; ++i)
+        {
+            d.fwdMat.push_back(d.timeline[i]);
+            d.discMat.push_back(NAN);
+            d.needNum.push_back(i > 0);
+            d.libEnd.push_back(i + 1 < n ? d.timeline[i + 1] : NAN);
+        }
+        d.labels = {"contingent bond " + fmt2(p.maturity) + " " + fmt2(p.coupon)};
+    }
     else
     {
         std::map<double, vector<double>> opts;  // store.h:184-205
@@ -487,9 +511,17 @@ ProductDef productDef(const orc_product& p)
     return d;
 }
 
-// Europeans payoff layout: per event, the strikes in insertion order (mcPrd.h:374-399).
+// Per-run product data of the payoffs: Europeans, per event the strikes in insertion order
+// (mcPrd.h:374-399); ContingentBond, the coverages of the periods (myDt, mcPrd.h:441-452).
 vector<vector<double>> europeansStrikes(const orc_product& p)
 {
+    if (p.kind == 3)
+    {
+        const ProductDef d = productDef(p);
+        vector<double> cov;
+        for (size_t i = 0; i + 1 < d.timeline.size(); ++i) cov.push_back(d.timeline[i + 1] - d.timeline[i]);
+        return {cov};
+    }
     std::map<double, vector<double>> opts;
     for (int i = 0; i < p.n; ++i) opts[p.mats[i]].push_back(p.strikes[i]);
     vector<vector<double>> s;
@@ -528,6 +560,23 @@ void payoffs(const orc_product& p, const vector<vector<double>>& estr, const Sam
         out[0] = alive * euro;
         out[1] = euro;
     }
+    else if (p.kind == 3)  // mcPrd.h:522-573
+    {
+        const double smooth = val(path[0].forward) * (p.smooth <= 0 ? 0.0 : p.smooth), twoSmooth = 2 * smooth;
+        T pay(0.0);
+        for (size_t i = 0; i + 1 < nEv; ++i)
+        {
+            const T& s0 = path[i].forward;
+            const T& s1 = path[i + 1].forward;
+            T digital;
+            if (val(s1) - val(s0) > smooth) digital = T(1.0);
+            else if (val(s1) - val(s0) < -smooth) digital = T(0.0);
+            else digital = (s1 - s0 + smooth) / twoSmooth;
+            pay += digital * (path[i].libor + p.coupon) * estr[0][i] / path[i + 1].numeraire;
+        }
+        pay += 1.0 / path[nEv - 1].numeraire;
+        out[0] = pay;
+    }
     else  // mcPrd.h:374-399
     {
         size_t k = 0;
@@ -550,7 +599,7 @@ struct ModelRun
     vector<double> tl;
     vector<int> common;  // Dupire: step index is a product date
     // BS precomputations
-    vector<T> stds, drifts, nums, discs, ffs;
+    vector<T> stds, drifts, nums, discs, ffs, libs;
     bool todayOn = false;
     // Dupire precomputations
     vector<double> logSpots;
@@ -617,6 +666,7 @@ struct ModelRun
             nums.assign(ne, T(1.0));
             discs.assign(ne, T(1.0));
             ffs.assign(ne, T(1.0));
+            libs.assign(ne, T(0.0));
             for (size_t e = 0; e < ne; ++e)
             {
                 const double t = pd->timeline[e];
@@ -624,6 +674,11 @@ struct ModelRun
                     nums[e] = m->spot_measure ? exp(params[3] * t) / params[0] : exp(params[2] * t);
                 if (!std::isnan(pd->discMat[e])) discs[e] = exp(-params[2] * (pd->discMat[e] - t));
                 ffs[e] = exp(mu * (pd->fwdMat[e] - t));
+                if (!pd->libEnd.empty() && !std::isnan(pd->libEnd[e]))  // mcMdlBS.h:266-272
+                {
+                    const double dt = pd->libEnd[e] - t;
+                    libs[e] = (exp(params[2] * dt) - 1.0) / dt;
+                }
             }
         }
         else
@@ -650,6 +705,7 @@ struct ModelRun
                 path[e].numeraire = pd->needNum[e] ? (m->spot_measure ? nums[e] * s : nums[e]) : T(1.0);
                 path[e].forward = s * ffs[e];
                 path[e].discount = discs[e];
+                path[e].libor = libs[e];
             };
             if (todayOn) fill(idx++, spot);
             for (size_t i = 0; i < simDim(); ++i)
@@ -667,6 +723,7 @@ struct ModelRun
             {
                 path[idx].numeraire = T(1.0);
                 path[idx].discount = T(1.0);
+                path[idx].libor = T(0.0);
                 path[idx++].forward = exp(logspot);
             }
             for (size_t i = 0; i < simDim(); ++i)
@@ -677,6 +734,7 @@ struct ModelRun
                 {
                     path[idx].numeraire = T(1.0);
                     path[idx].discount = T(1.0);
+                    path[idx].libor = T(0.0);
                     path[idx++].forward = exp(logspot);
                 }
             }
@@ -695,7 +753,7 @@ std::unique_ptr<Rng> makeRng(int sobol, unsigned s1, unsigned s2, int dim)
     return std::unique_ptr<Rng>(new Mrg(s1, s2, dim));
 }
 
-int nPayoffs(const orc_product& p) { return p.kind == 0 ? 1 : p.kind == 1 ? 2 : p.n; }
+int nPayoffs(const orc_product& p) { return p.kind == 0 || p.kind == 3 ? 1 : p.kind == 1 ? 2 : p.n; }
 
 // Serial path loop (mcBase.h:267-308) over paths [first, first+count).
 void runPaths(const orc_model& m, const orc_product& p, int sobol, unsigned s1, unsigned s2, uint64_t first,
@@ -1196,7 +1254,7 @@ int orc_risk_multi(const orc_model* m, const orc_product* p, int sobol, int nPat
 int orc_risk_fast(const orc_model* m, const orc_product* p, int sobol, int nPath, unsigned s1, unsigned s2,
                   const double* weights, int nThreads, double* values, double* aggValue, double* risks)
 {
-    if (m->kind != 1) return orc_risk(m, p, sobol, nPath, s1, s2, weights, values, aggValue, risks);
+    if (m->kind != 1 || p->kind == 3) return orc_risk(m, p, sobol, nPath, s1, s2, weights, values, aggValue, risks);
     const int nPay = nPayoffs(*p);
     const size_t nParam = 1 + size_t(m->nS) * m->nT;
     auto rg = ranges(uint64_t(nPath), std::max(1, nThreads));

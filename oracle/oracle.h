@@ -31,15 +31,18 @@ typedef struct {
     double maxdt;
 } orc_model;
 
-/* Product description (mcPrd.h): European, up-and-out call/put, portfolio of Europeans. */
+/* Product description (mcPrd.h): European, up-and-out call/put, portfolio of Europeans,
+ * contingent bond. */
 typedef struct {
-    int kind;               /* 0 = European, 1 = UOC, 2 = Europeans */
+    int kind;               /* 0 = European, 1 = UOC, 2 = Europeans, 3 = ContingentBond */
     double strike, exercise, settlement;             /* European */
-    double barrier, maturity, freq, smooth;          /* UOC (strike shared); smooth as given to putBarrier */
+    double barrier, maturity, freq, smooth;          /* UOC (strike shared); smooth as given to putBarrier;
+                                                        ContingentBond: maturity, payment frequency, smooth */
     int callput;
     int n;                  /* Europeans: n (maturity, strike) pairs */
     const double* mats;
     const double* strikes;
+    double coupon;          /* ContingentBond */
 } orc_product;
 
 /* Shapes: number of payoffs, parameters, Gaussians per path (simDim). */

@@ -277,6 +277,13 @@ int main()
             double K = rd(std::cin), te = rd(std::cin), ts = rd(std::cin);
             putEuropean(K, te, ts, id);
         }
+        else if (cmd == "contingent")  // id coupon maturity payFreq smooth
+        {
+            string id;
+            std::cin >> id;
+            double cpn = rd(std::cin), mat = rd(std::cin), fq = rd(std::cin), sm = rd(std::cin);
+            putContingent(cpn, mat, fq, sm, id);
+        }
         else if (cmd == "uoc")  // id K B T freq smooth callput
         {
             string id;

@@ -7,7 +7,7 @@ AADriskAggregate, AADriskMulti, bumpRisk, dupireCalib, dupireSuperbucket, the RN
 Every case records its inputs next to its outputs, so the fixtures are self-contained:
 the tests never need the reference.
 
-    python3 tests/golden/make_golden.py [rng host mc calib bump]   # all when none named;
+    python3 tests/golden/make_golden.py [rng host mc calib bump products]   # all when none named;
                                                                    # rebuilds the driver when missing
 """
 import json
@@ -113,6 +113,8 @@ def model_cmd(mid, m):
 
 
 def product_cmd(pid, p):
+    if p["kind"] == "contingent":
+        return f"contingent {pid} {f(p['coupon'])} {f(p['maturity'])} {f(p['freq'])} {f(p['smooth'])}"
     if p["kind"] == "european":
         return f"european {pid} {f(p['strike'])} {f(p['exercise'])} {f(p['settlement'])}"
     if p["kind"] == "uoc":
@@ -326,6 +328,45 @@ def bump_cases(models, products):
     return out
 
 
+def product_cases(models):
+    """The contingent bond (mcPrd.h:404-574): pays (libor + coupon) x coverage at the end of each
+    period whose spot rose (a smoothed digital), plus the redemption; on Black-Scholes (risk-
+    neutral and spot measure: libors and numeraires) and Dupire (no rates).  value, AADriskOne
+    and bumpRisk through the reference."""
+    products = {"cbond": dict(kind="contingent", coupon=0.02, maturity=3.0, freq=0.25, smooth=0.05),
+                "cbond_sharp": dict(kind="contingent", coupon=0.035, maturity=2.0, freq=0.5, smooth=0.0),
+                "cbond_monthly": dict(kind="contingent", coupon=0.01, maturity=1.0, freq=1.0 / 12.0, smooth=0.02)}
+    cases = [("bs_cbond_mrg", "bs", "cbond", 0, 4096), ("bs_cbond_sobol", "bs", "cbond", 1, 2048),
+             ("bs_rates_cbond_monthly", "bs_rates", "cbond_monthly", 0, 2048),
+             ("bs_spotmeasure_cbond", "bs_spotmeasure", "cbond", 1, 2048),
+             ("bs_cbond_sharp", "bs_rates", "cbond_sharp", 0, 2048),
+             ("dup20x10_cbond", "dup20x10", "cbond", 0, 2048), ("dup60x30_monthly_cbond", "dup60x30_monthly",
+                                                                 "cbond_monthly", 1, 1024)]
+    used = {c[1] for c in cases}
+    cmds = [model_cmd(mid, m) for mid, m in models.items() if mid in used] + \
+           [product_cmd(pid, p) for pid, p in products.items()]
+    for (_, mid, pid, sob, n) in cases:
+        cmds += [f"value {mid} {pid} {num(sob, n)}", f"risk {mid} {pid} {num(sob, n)} 0",
+                 f"bump {mid} {pid} {num(sob, min(n, 512))}"]
+    it = iter(run(cmds))
+    out = {"models": {k: v for k, v in models.items() if k in used}, "products": products, "cases": []}
+    for (name, mid, pid, sob, n) in cases:
+        rec = dict(name=name, model=mid, product=pid, sobol=sob, npath=n, bump_npath=min(n, 512),
+                   seed1=12345, seed2=1234)
+        rec["values"] = next(it)[1]
+        next(it)
+        next(it)  # risk: values
+        rec["risk_value"] = next(it)[1][0]
+        rec["risks"] = next(it)[1]
+        next(it)
+        next(it)  # bump: values
+        rec["bump_risks"] = next(it)[1]
+        next(it)
+        next(it)
+        out["cases"].append(rec)
+    return out
+
+
 def calib_cases():
     out = {}
     incl_spots, maxds, incl_times, maxdtv = W.superbucket_grid(60, 30)
@@ -385,7 +426,7 @@ def main():
     only = set(sys.argv[1:])
     for name, fn in [("rng", rng_cases), ("host", lambda: host_cases(models, products)),
                      ("mc", lambda: mc_cases(models, products)), ("calib", calib_cases),
-                     ("bump", lambda: bump_cases(models, products))]:
+                     ("bump", lambda: bump_cases(models, products)), ("products", lambda: product_cases(models))]:
         if only and name not in only:
             continue
         obj = fn()

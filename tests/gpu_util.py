@@ -21,6 +21,8 @@ def put_model(eng, mid, spec):
 def put_product(eng, pid, spec):
     if spec["kind"] == "european":
         eng.putEuropean(spec["strike"], spec["exercise"], spec["settlement"], pid)
+    elif spec["kind"] == "contingent":
+        eng.putContingent(spec["coupon"], spec["maturity"], spec["freq"], spec["smooth"], pid)
     elif spec["kind"] == "uoc":
         eng.putBarrier(spec["strike"], spec["barrier"], spec["maturity"], spec["freq"], spec["smooth"],
                        spec.get("callput", 0), pid)

@@ -161,3 +161,15 @@ def test_superbucket(golden):
         if "microbucket" in c:
             assert rel(mb, c["microbucket"]) < 1e-13
         assert rel(vega, c["vega"]) < 2e-5, c["name"]
+
+
+def test_contingent_bond(golden):
+    """The contingent bond (mcPrd.h:404-574) in the restatement against the reference: values
+    and tape risks (rates through the libors and numeraires on Black-Scholes)."""
+    d = golden("products")
+    for c in d["cases"]:
+        m, p = O.Model(d["models"][c["model"]]), O.Product(d["products"][c["product"]])
+        v, _ = O.value(m, p, c["sobol"], c["npath"])
+        assert rel(v, c["values"]) < 1e-13, c["name"]
+        vv, agg, r = O.risk(m, p, c["sobol"], c["npath"], np.array([1.0]))
+        assert rel(r, c["risks"]) < 1e-12, c["name"]

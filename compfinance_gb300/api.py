@@ -79,6 +79,8 @@ class Engine:
         h = ctypes.c_void_p()
         _check(lib().cf_create(int(device), ctypes.byref(h)))
         self._h = h
+        # labels of stored models and products, dropped when the id is stored again
+        self._label_cache = {}
 
     def close(self):
         if self._h:
@@ -106,6 +108,7 @@ class Engine:
     def putBlackScholes(self, spot, vol, qSpot, rate, div, id):
         _check(lib().cf_put_black_scholes(self._h, ctypes.c_double(spot), ctypes.c_double(vol), int(bool(qSpot)),
                                           ctypes.c_double(rate), ctypes.c_double(div), id.encode()))
+        self._label_cache.pop(("m", id), None)
         return id
 
     def putDupire(self, spot, spots, times, vols, maxDt, id):
@@ -115,6 +118,7 @@ class Engine:
             raise CfError(-1, "putDupire: vols must be len(spots) x len(times)")
         _check(lib().cf_put_dupire(self._h, ctypes.c_double(spot), _p(s), len(s), _p(t), len(t), _p(v),
                                    ctypes.c_double(maxDt), id.encode()))
+        self._label_cache.pop(("m", id), None)
         return id
 
     def putEuropean(self, strike, exerciseDate, settlementDate=None, id="european"):
@@ -122,25 +126,35 @@ class Engine:
             settlementDate = exerciseDate
         _check(lib().cf_put_european(self._h, ctypes.c_double(strike), ctypes.c_double(exerciseDate),
                                      ctypes.c_double(settlementDate), id.encode()))
+        self._label_cache.pop(("p", id), None)
         return id
 
     def putBarrier(self, strike, barrier, maturity, monitorFreq, smooth, callPut, id):
         _check(lib().cf_put_barrier(self._h, ctypes.c_double(strike), ctypes.c_double(barrier),
                                     ctypes.c_double(maturity), ctypes.c_double(monitorFreq), ctypes.c_double(smooth),
                                     int(bool(callPut)), id.encode()))
+        self._label_cache.pop(("p", id), None)
         return id
 
     def putContingent(self, coupon, maturity, payFreq, smooth, id):
         """store.h:165-180: the contingent bond of mcPrd.h:404-574."""
         _check(lib().cf_put_contingent(self._h, ctypes.c_double(coupon), ctypes.c_double(maturity),
                                        ctypes.c_double(payFreq), ctypes.c_double(smooth), id.encode()))
+        self._label_cache.pop(("p", id), None)
 
     def putEuropeans(self, maturities, strikes, id):
         m, k = _arr(maturities), _arr(strikes)
         _check(lib().cf_put_europeans(self._h, _p(m), _p(k), len(m), id.encode()))
+        self._label_cache.pop(("p", id), None)
         return id
 
-    def _labels(self, fn, key):
+    def _labels(self, fn, key, kind):
+        got = self._label_cache.get((kind, key))
+        if got is None:
+            got = self._label_cache[(kind, key)] = self._fetch_labels(fn, key)
+        return list(got)
+
+    def _fetch_labels(self, fn, key):
         n, need = ctypes.c_int(), ctypes.c_size_t()
         _check(fn(self._h, key.encode(), None, ctypes.c_size_t(0), ctypes.byref(n), ctypes.byref(need)))
         buf = ctypes.create_string_buffer(need.value)
@@ -149,10 +163,10 @@ class Engine:
         return s.split("\n") if s else []
 
     def payoffLabels(self, productId):
-        return self._labels(lib().cf_payoff_labels, productId)
+        return self._labels(lib().cf_payoff_labels, productId, "p")
 
     def parameterLabels(self, modelId):
-        return self._labels(lib().cf_parameter_labels, modelId)
+        return self._labels(lib().cf_parameter_labels, modelId, "m")
 
     def shapes(self, modelId, productId):
         a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
@@ -229,7 +243,7 @@ class Engine:
 
     def AADriskMulti(self, modelId, productId, num):
         npay, npar, _ = self.shapes(modelId, productId)
-        v, r = np.zeros(npay), np.zeros(npar * npay)
+        v, r = np.empty(npay), np.empty(npar * npay)  # every entry is written
         nc = num.c()
         _check(lib().cf_aad_risk_multi(self._h, modelId.encode(), productId.encode(), ctypes.byref(nc), _p(v),
                                        _p(r)))

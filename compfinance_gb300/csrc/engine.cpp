@@ -449,6 +449,10 @@ int Context::buildPlan(const ModelDesc& m, const ProductDesc& pd, Plan& plan)
             P.nodeShiftF = std::min(FIX_HI_SHIFT, shift);
             P.fast32 = (pd.kind == PROD_UOC || pd.kind == PROD_EUROPEAN) && evOk && nS <= 510 && minGap > 0 &&
                        range / nBf <= minGap / 1.5 && shift >= 4;
+            // FP32 AADriskMulti (multi_risk32.cu) uses the same tables and slab unit: its chunks
+            // hold 256 paths of one bucket
+            plan.multi32 = pd.kind == PROD_EUROPEANS && nS <= 510 && minGap > 0 && range / nBf <= minGap / 1.5 &&
+                           shift >= 4;
             P.nBucketsF = nBf;
             P.bX0F = Xf[0];
             P.bInvWF = float(1.0 / wf);
@@ -752,11 +756,21 @@ size_t Context::footprint(const Plan& plan, const cf_num_param& num, bool risk) 
     if (mc_occupancy(l, smem, &occ) || occ < 1) occ = 16;
     const long long needed = sobol ? (num.numPath / 32 + 1) * 32 : (num.numPath + 1) / 2;
     const long long threads = std::min<long long>(needed, (long long)numSMs * occ * 128);
+    if (plan.prod == PROD_EUROPEANS && risk && multi32Use(plan, num))
+    {
+        // multi_risk32.cu: step records per path, bucket and spot per (maturity, path), entry
+        // lists, bucket accumulators and the finished risks
+        const size_t nP = size_t(num.numPath), nE = size_t(plan.nEv);
+        return nP * size_t((plan.nSteps + 1) & ~1) * 8 + nE * nP * 14 +
+               size_t(plan.nPay + plan.nEv) * size_t(plan.nParam) * 16 + size_t(plan.nPay) * size_t(plan.nParam) * 8 +
+               size_t(plan.nPay + plan.nEv) * 96 + 8192;
+    }
     const int fields = plan.prod == PROD_EUROPEANS ? 1 + 3 * NP : mc_scratch_fields(l);
     size_t b = size_t(plan.nParam + 2 * plan.nPay + 2) * 16 + size_t(plan.nPay) * 12 + 4096;
     if (risk) b += size_t(fields) * size_t(plan.nSteps + 1) * size_t(threads) * (fp32 ? 4 : 8);
     if (risk && l.fast) b += size_t((threads + 127) / 128) * size_t(plan.base.nS) * size_t(plan.base.nT) * 8 + 256;
-    if (plan.prod == PROD_EUROPEANS && risk) b += size_t(plan.nPay + plan.nEv) * size_t(plan.nParam) * 16;
+    // multi: bucket accumulators plus the finished per-payoff risks
+    if (plan.prod == PROD_EUROPEANS && risk) b += size_t(plan.nPay + plan.nEv) * size_t(plan.nParam) * 16 + size_t(plan.nPay) * size_t(plan.nParam) * 8;
     return b;
 }
 

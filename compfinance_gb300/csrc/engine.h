@@ -66,6 +66,7 @@ struct Plan
 {
     int model = 0, prod = 0, nSteps = 0, nEv = 0, nPay = 0, nParam = 0;
     bool sobolOk = false;
+    bool multi32 = false;  // European portfolio on Dupire with the FP32 tables: multi_risk32.cu
     size_t yBytesD = 0, yBytesF = 0;
     unsigned long long mver = 0, pver = 0;
     std::vector<double> timeline;
@@ -141,7 +142,9 @@ struct Context
     size_t footprint(const Plan& plan, const cf_num_param& num, bool risk) const;
     // AADriskMulti: the multi kernel (European portfolios) is asynchronous like enqueue
     bool multiFast(const Plan& plan) const;
-    int enqueueMulti(Slot& slot, Plan& plan, const cf_num_param& num);
+    bool multi32Use(const Plan& plan, const cf_num_param& num) const;  // FP32 Dupire: multi_risk32.cu
+    // directRisks: the caller's nParam x nPay array, written before the call returns
+    int enqueueMulti(Slot& slot, Plan& plan, const cf_num_param& num, double* directRisks = nullptr);
     int finishMulti(Slot& slot, double* values, double* risks);
     int riskMulti(Plan& plan, const cf_num_param& num, double* values, double* risks);
     // main-slot conveniences of the synchronous API

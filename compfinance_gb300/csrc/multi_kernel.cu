@@ -7,8 +7,8 @@
 // payoffs a path pays are the m_e strikes below F_e, and
 //     d payoff_(e,j) / d theta = a_theta - K_j b_theta   for j < m_e, 0 otherwise,
 // with a = dF/dtheta / N - F dN/dtheta / N^2 and b = -dN/dtheta / N^2 path quantities.  The
-// kernel accumulates a and b into bucket (e, m_e); the host turns buckets into per-strike
-// sums by suffix sums over m.  Values and squares use the same buckets.
+// kernel accumulates a and b into bucket (e, m_e); multi_finish turns buckets into per-strike
+// risks by suffix sums over m.  Values and squares use the same buckets.
 //
 // Dupire: a = S_e dx_e/dtheta (N = 1), from a reverse sweep that carries one adjoint per
 // maturity.  Black-Scholes: four parameters, forward tangents of log S.
@@ -349,6 +349,56 @@ int multi_occupancy(int model, int rng, int fp32, size_t smem, int* occ)
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return (int)e;
     return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, fn, MC_BLOCK, smem);
+}
+
+// Per-payoff risks from the bucket accumulators.  Bucket m of a maturity holds the adjoints of
+// the paths whose spot lies between its (m-1)th and mth sorted strikes, so the payoff of the
+// jth strike collects the buckets above j: thread (q, e) (one model parameter, one maturity)
+// walks the maturity's buckets from the top, keeps exact integer suffix sums and writes
+// risk[q][payoff] = sum / nPath.  Black-Scholes buckets hold a pair (a, b) per parameter and the
+// strike's risk is (a - K b) / nPath.
+__global__ void multi_finish(const long long* __restrict__ accR, int nAccParam, int nOut, const int* __restrict__ evOff,
+                             const double* __restrict__ ks, const int* __restrict__ orig, int nPay, int bs, double n,
+                             double* __restrict__ risks)
+{
+    const int q = blockIdx.x * blockDim.x + threadIdx.x, ev = blockIdx.y;
+    if (q >= nOut) return;
+    auto val = [](long long hi, long long lo) {
+        return __dadd_rn(__dmul_rn((double)hi, 1.0 / 1048576.0), __dmul_rn((double)lo, 1.0 / 1152921504606846976.0));
+    };
+    const int b0 = evOff[ev], nK = evOff[ev + 1] - b0 - 1, sorted = b0 - ev;
+    long long ha = 0, la = 0, hb = 0, lb = 0;
+#pragma unroll 4
+    for (int j = nK - 1; j >= 0; --j)
+    {
+        const size_t bk = size_t(b0 + j + 1);
+        double r;
+        if (bs)
+        {
+            const long long* a = accR + 2 * (bk * nAccParam + 2 * q);
+            ha += a[0];
+            la += a[1];
+            hb += a[2];
+            lb += a[3];
+            r = __ddiv_rn(__dsub_rn(val(ha, la), __dmul_rn(ks[sorted + j], val(hb, lb))), n);
+        }
+        else
+        {
+            const long long* a = accR + 2 * (bk * nAccParam + q);
+            ha += a[0];
+            la += a[1];
+            r = __ddiv_rn(val(ha, la), n);
+        }
+        risks[size_t(q) * nPay + orig[sorted + j]] = r;
+    }
+}
+
+int launch_multi_finish(const long long* accR, int nAccParam, int nOut, int nEv, const int* evOff, const double* ks,
+                        const int* orig, int nPay, int bs, double n, double* risks, void* stream)
+{
+    multi_finish<<<dim3((nOut + 127) / 128, nEv), 128, 0, (cudaStream_t)stream>>>(accR, nAccParam, nOut, evOff, ks, orig,
+                                                                                nPay, bs, n, risks);
+    return (int)cudaGetLastError();
 }
 
 int launch_multi(int model, int rng, int fp32, int grid, size_t smem, const MultiParams& mp, void* stream)

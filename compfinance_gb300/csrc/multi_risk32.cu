@@ -41,7 +41,6 @@ constexpr int LO_SHIFT = T_BITS + 1;
 constexpr unsigned TWO_BITS = 0x40000000u;         // bits of 2.0f; t + 2 in [2, 3)
 constexpr float T_MAX = 1.0f - 1.0f / 4194304.0f;
 constexpr float AV_MAX = 512.0f;  // larger contributions go exactly to the global accumulators
-static_assert(M32_CHUNK == 2 * MB, "a reverse thread sweeps two entries of a chunk");
 
 __host__ __device__ inline size_t a16(size_t x) { return (x + 15) & ~size_t(15); }
 
@@ -424,18 +423,12 @@ __global__ void __launch_bounds__(MB) multi32_reverse(const Multi32Args A)
         const int count = end - first < M32_CHUNK ? end - first : M32_CHUNK;
         long long* row = A.accRisk + 2 * size_t(b) * A.nParam;
 
-        // thread tid sweeps entries tid and tid + MB of the chunk side by side (two independent
-        // adjoint chains; a missing second entry replays the first one's records with adjoint 0)
-        if (tid < count)
+        for (int idx = tid; idx < count; idx += MB)
         {
-            const bool two = tid + MB < count;
-            const int* e0 = A.list + 2 * (first + tid);
-            const int* e1 = two ? e0 + 2 * MB : e0;
-            float ax0 = __int_as_float(__ldg(e0 + 1));  // d payoff / d x_e = S_e
-            float ax1 = two ? __int_as_float(__ldg(e1 + 1)) : 0.0f;
-            const uint4* r0 = reinterpret_cast<const uint4*>(A.rec + 2 * size_t(__ldg(e0)) * A.pitch);
-            const uint4* r1 = reinterpret_cast<const uint4*>(A.rec + 2 * size_t(__ldg(e1)) * A.pitch);
-            auto step = [&](float& ax, int s, unsigned W, unsigned gbits) {
+            const int path = __ldg(A.list + 2 * (first + idx));
+            float ax = __int_as_float(__ldg(A.list + 2 * (first + idx) + 1));  // d payoff / d x_e = S_e
+            const uint4* rr = reinterpret_cast<const uint4*>(A.rec + 2 * size_t(path) * A.pitch);
+            auto step = [&](int s, unsigned W, unsigned gbits) {
                 const float ga = __uint_as_float(gbits);
                 const int l = int(W >> LO_SHIFT);
                 const float t = __uint_as_float(TWO_BITS | (W & T_MASK)) - 2.0f;
@@ -446,7 +439,7 @@ __global__ void __launch_bounds__(MB) multi32_reverse(const Multi32Args A)
                 ax += av * (yd.y * ir.y);        // d x_{s+1} / d x_s = 1 + (g - v) dv/dx
                 if (av == 0.0f) return;
                 const int jl = l - (l > 0 ? 1 : 0);
-                const bool inner = l > 0 && l < nS;
+                const bool inner = l > 0 && l < nS;  // two spot knots; one at the flat ends
                 const float cR = av * t, cL = av - cR;
                 const int4 sc = stepc[s];
                 if (fabsf(av) < AV_MAX)
@@ -473,36 +466,27 @@ __global__ void __launch_bounds__(MB) multi32_reverse(const Multi32Args A)
                     }
                 }
             };
-            // steps iE-1 .. 0, stored in pairs (2k, 2k+1); the next pairs are loaded one ahead
+            // steps iE-1 .. 0, stored in pairs (2k, 2k+1); the next pair is loaded one ahead
             int s = iE - 1;
             if (s >= 0)
             {
-                uint4 c0 = __ldg(r0 + (s >> 1)), c1 = __ldg(r1 + (s >> 1));
+                uint4 cur = __ldg(rr + (s >> 1));
                 for (;;)
                 {
                     const int k = s >> 1;
-                    uint4 n0 = make_uint4(0u, 0u, 0u, 0u), n1 = n0;
-                    if (k > 0)
-                    {
-                        n0 = __ldg(r0 + k - 1);
-                        n1 = __ldg(r1 + k - 1);
-                    }
+                    const uint4 nxt = k > 0 ? __ldg(rr + k - 1) : make_uint4(0u, 0u, 0u, 0u);
                     if (s & 1)
                     {
-                        step(ax0, s, c0.z, c0.w);
-                        step(ax1, s, c1.z, c1.w);
+                        step(s, cur.z, cur.w);
                         --s;
                     }
-                    step(ax0, s, c0.x, c0.y);
-                    step(ax1, s, c1.x, c1.y);
+                    step(s, cur.x, cur.y);
                     --s;
                     if (s < 0) break;
-                    c0 = n0;
-                    c1 = n1;
+                    cur = nxt;
                 }
             }
-            fix_add(spotSlab, ax0 / spot);  // x_0 = log(spot)
-            if (two) fix_add(spotSlab, ax1 / spot);
+            fix_add(spotSlab, ax / spot);  // x_0 = log(spot)
         }
         __syncthreads();
         // the chunk's slab -> the bucket's row (node words in units of 2^-nodeShiftF: exact in hi)

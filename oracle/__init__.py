@@ -251,3 +251,115 @@ def fill(x, maxdx, mindx, add=()):
     out, po = _arr(np.zeros(n))
     lib().orc_fill(px, len(xa), ctypes.c_double(maxdx), ctypes.c_double(mindx), pa, len(add), po)
     return out
+
+
+# ---- multi-asset displaced model and products (mcMdlMultiDisplaced.h, mcPrdMulti.h) ----
+class OrcMModel(ctypes.Structure):
+    _fields_ = [("nA", ctypes.c_int), ("disc", ctypes.c_double), ("spots", _dp), ("spreads", _dp),
+                ("nDiv", ctypes.c_int), ("divDates", _dp), ("divs", _dp), ("atms", _dp), ("skews", _dp),
+                ("correl", _dp), ("lambda_", ctypes.c_double)]
+
+
+class OrcMProduct(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int), ("nA", ctypes.c_int), ("weights", _dp), ("maturity", ctypes.c_double),
+                ("nK", ctypes.c_int), ("strikes", _dp), ("refs", _dp), ("periods", ctypes.c_int),
+                ("ko", ctypes.c_double), ("strike", ctypes.c_double), ("cpn", ctypes.c_double),
+                ("smooth", ctypes.c_double)]
+
+
+class MModel:
+    """spec: assets, spots, atms, skews, disc, spreads, div_dates, divs [nDiv][nA], correl [nA][nA], lambda."""
+
+    def __init__(self, spec):
+        self.spec = spec
+        n = len(spec["assets"])
+        self._keep = []
+        m = OrcMModel()
+        m.nA, m.disc, m.lambda_ = n, spec["disc"], spec["lambda"]
+
+        def arr(x):
+            a, p = _arr(np.asarray(x, dtype=float).reshape(-1) if np.size(x) else [0.0])
+            self._keep.append(a)
+            return p
+        m.spots, m.spreads = arr(spec["spots"]), arr(spec["spreads"])
+        m.atms, m.skews = arr(spec["atms"]), arr(spec["skews"])
+        m.nDiv = len(spec["div_dates"])
+        m.divDates, m.divs = arr(spec["div_dates"]), arr(spec["divs"])
+        m.correl = arr(spec["correl"])
+        self.c = m
+
+
+class MProduct:
+    """spec kind 'baskets' (assets, weights, maturity, strikes) or 'autocall' (assets, refs,
+    maturity, periods, ko, strike, cpn, smooth)."""
+
+    def __init__(self, spec):
+        self.spec = spec
+        self._keep = []
+        p = OrcMProduct()
+        p.nA = len(spec["assets"])
+
+        def arr(x):
+            a, q = _arr(x)
+            self._keep.append(a)
+            return q
+        if spec["kind"] == "baskets":
+            p.kind = 0
+            p.weights, p.maturity = arr(spec["weights"]), spec["maturity"]
+            p.nK, p.strikes = len(spec["strikes"]), arr(spec["strikes"])
+        else:
+            p.kind = 1
+            p.refs, p.maturity, p.periods = arr(spec["refs"]), spec["maturity"], int(spec["periods"])
+            p.ko, p.strike, p.cpn, p.smooth = spec["ko"], spec["strike"], spec["cpn"], spec["smooth"]
+        self.c = p
+
+
+def m_shapes(model, product):
+    a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    lib().orc_m_shapes(ctypes.byref(model.c), ctypes.byref(product.c), ctypes.byref(a), ctypes.byref(b),
+                       ctypes.byref(c))
+    return a.value, b.value, c.value
+
+
+def m_value(model, product, sobol, npath, seed1=12345, seed2=1234):
+    npay, _, _ = m_shapes(model, product)
+    v, pv = _arr(np.zeros(npay))
+    e, pe = _arr(np.zeros(npay))
+    assert lib().orc_m_value(ctypes.byref(model.c), ctypes.byref(product.c), int(sobol), int(npath), seed1, seed2,
+                             pv, pe) == 0
+    return v, e
+
+
+def m_risk(model, product, sobol, npath, weights, seed1=12345, seed2=1234):
+    npay, npar, _ = m_shapes(model, product)
+    w, pw = _arr(weights)
+    v, pv = _arr(np.zeros(npay))
+    r, pr = _arr(np.zeros(npar))
+    agg = ctypes.c_double()
+    assert lib().orc_m_risk(ctypes.byref(model.c), ctypes.byref(product.c), int(sobol), int(npath), seed1, seed2,
+                            pw, pv, ctypes.byref(agg), pr) == 0
+    return v, agg.value, r
+
+
+def m_risk_multi(model, product, sobol, npath, seed1=12345, seed2=1234):
+    npay, npar, _ = m_shapes(model, product)
+    v, pv = _arr(np.zeros(npay))
+    r, pr = _arr(np.zeros(npar * npay))
+    assert lib().orc_m_risk_multi(ctypes.byref(model.c), ctypes.byref(product.c), int(sobol), int(npath), seed1,
+                                  seed2, pv, pr) == 0
+    return v, r.reshape(npar, npay)
+
+
+def m_init(model, product):
+    """(chol, stds, drifts, ffs, alphas, dynamics, numeraires) after the model's init."""
+    n = len(model.spec["assets"])
+    _, _, dim = m_shapes(model, product)
+    ns = dim // n
+    nev = 1 if product.spec["kind"] == "baskets" else int(product.spec["periods"])
+    out = [np.zeros(n * n), np.zeros(ns * n), np.zeros(ns * n), np.zeros(ns * n), np.zeros(n)]
+    ptr = [o.ctypes.data_as(_dp) for o in out]
+    dyn = np.zeros(n, dtype=np.int32)
+    nums = np.zeros(nev)
+    assert lib().orc_m_init(ctypes.byref(model.c), ctypes.byref(product.c), *ptr,
+                            dyn.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), nums.ctypes.data_as(_dp)) == 0
+    return out[0].reshape(n, n), out[1].reshape(ns, n), out[2].reshape(ns, n), out[3].reshape(ns, n), out[4], dyn, nums

@@ -7,6 +7,7 @@
 #include "oracle.h"
 
 #include <algorithm>
+#include <stdexcept>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -1164,6 +1165,348 @@ vector<T> calibrate(const orc_ivs& s, const CalibGrid& g, const RiskViewT<T>& rv
 // =======================================================================================
 // C API
 // =======================================================================================
+
+namespace {
+
+// ---------------------------------------------------------------------------------------
+// Multiple correlated assets, displaced Black-Scholes dynamics with proportional dividends
+// (mcMdlMultiDisplaced.h:28-717, Cholesky of choldc.h:8-49), with the products Baskets
+// and Autocall (mcPrdMulti.h:181-439).  Generic in T (double, or Var on the tape).
+// ---------------------------------------------------------------------------------------
+enum MdDyn { MD_LOG = 0, MD_NORMAL = 1, MD_SUR = 2, MD_SUB = 3 };
+inline double mSqrt(double x) { return std::sqrt(x); }
+inline Var mSqrt(const Var& x) { return sqrt(x); }
+
+// Product timeline and numeraire flags (mcPrdMulti.h:201-216, 301-316).
+vector<double> mTimeline(const orc_mproduct& p)
+{
+    if (p.kind == 0) return {p.maturity};
+    vector<double> tl;
+    double t = 0.0;
+    const double dt = p.maturity / p.periods;
+    for (int k = 0; k < p.periods; ++k)
+    {
+        t += dt;
+        tl.push_back(t);
+    }
+    return tl;
+}
+
+int mPayoffs(const orc_mproduct& p) { return p.kind == 0 ? p.nK : 1; }
+size_t mParams(const orc_mmodel& m)
+{
+    const size_t n = size_t(m.nA);
+    return 1 + 2 * n + n * size_t(m.nDiv) + 2 * n + n * (n - 1) / 2 + 1;
+}
+
+template <class T>
+struct MdRun
+{
+    const orc_mmodel* m;
+    vector<double> ptl;  // product timeline
+    vector<double> tl;   // simulation timeline: today + product dates after today
+    bool todayOn = false;
+    vector<T> params;
+    // parameters, by role (copies of params entries)
+    T disc, lambda;
+    vector<T> spot, spread, atm, skew, divs, correl;  // divs [nDiv][nA], correl [nA][nA] lower
+    // init outputs
+    vector<T> chol, stds, drifts, ffs, alphas, nums;
+    vector<int> dyn;
+
+    void allocate(const orc_mmodel& mm, const orc_mproduct& p)  // mcMdlMultiDisplaced.h:367-405
+    {
+        m = &mm;
+        ptl = mTimeline(p);
+        tl = {0.0};
+        for (double t : ptl)
+            if (t > 0.0) tl.push_back(t);
+        todayOn = ptl[0] == 0.0;
+    }
+    size_t nSteps() const { return tl.size() - 1; }
+
+    // Parameter order of the reference (mcMdlMultiDisplaced.h:146-209).
+    void putParams(bool onTape)
+    {
+        const int n = m->nA;
+        params.clear();
+        auto mk = [&](double x) {
+            params.push_back(onTape ? T(leafOf(x)) : T(x));
+            return params.back();
+        };
+        disc = mk(m->disc);
+        spot.clear(); spread.clear(); atm.clear(); skew.clear(); divs.clear();
+        for (int a = 0; a < n; ++a) spot.push_back(mk(m->spots[a]));
+        for (int a = 0; a < n; ++a) spread.push_back(mk(m->spreads[a]));
+        for (int d = 0; d < m->nDiv; ++d)
+            for (int a = 0; a < n; ++a) divs.push_back(mk(m->divs[size_t(d) * n + a]));
+        for (int a = 0; a < n; ++a) atm.push_back(mk(m->atms[a]));
+        for (int a = 0; a < n; ++a) skew.push_back(mk(m->skews[a]));
+        correl.assign(size_t(n) * n, T(0.0));
+        for (int i = 1; i < n; ++i)
+            for (int j = 0; j < i; ++j) correl[size_t(i) * n + j] = mk(m->correl[size_t(i) * n + j]);
+        lambda = mk(m->lambda);
+    }
+    static T leafOf(double x);
+
+    void init()  // mcMdlMultiDisplaced.h:407-566
+    {
+        const int n = m->nA;
+        vector<T> repo(n), beta(n);
+        for (int a = 0; a < n; ++a) repo[a] = disc - spread[a];
+        alphas.assign(n, T(0.0));
+        dyn.assign(n, MD_LOG);
+        for (int a = 0; a < n; ++a)  // displacement from ATM and skew (mcMdlMultiDisplaced.h:418-444)
+        {
+            beta[a] = atm[a] + 2 * skew[a];
+            if (std::fabs(val(skew[a])) < 1.0e-05)
+            {
+                dyn[a] = MD_LOG;
+                alphas[a] = T(0.0);
+            }
+            else if (std::fabs(val(beta[a])) < 1.0e-05)
+            {
+                dyn[a] = MD_NORMAL;
+                alphas[a] = -2 * spot[a] * skew[a];
+                beta[a] = T(0.0);
+            }
+            else if (val(beta[a]) > 0)
+            {
+                dyn[a] = MD_SUR;
+                alphas[a] = -2 * spot[a] / beta[a] * skew[a];
+            }
+            else
+            {
+                dyn[a] = MD_SUB;
+                beta[a] = -1.0 * beta[a];
+                alphas[a] = -2 * spot[a] / beta[a] * skew[a];
+            }
+        }
+        // symmetric correl with unit diagonal, lambda shift, Cholesky (choldc.h:8-49)
+        vector<T> used(size_t(n) * n);
+        for (int i = 0; i < n; ++i)
+            for (int j = 0; j < n; ++j)
+            {
+                const T raw = i == j ? T(1.0) : i > j ? correl[size_t(i) * n + j] : correl[size_t(j) * n + i];
+                used[size_t(i) * n + j] = lambda * (1.0 - raw) + raw;
+            }
+        chol.assign(size_t(n) * n, T(0.0));
+        for (int i = 0; i < n; ++i)
+            for (int j = 0; j <= i; ++j)
+            {
+                T sum = used[size_t(i) * n + j];
+                for (int k = 0; k < j; ++k) sum = sum - chol[size_t(i) * n + k] * chol[size_t(j) * n + k];
+                if (i == j)
+                {
+                    if (val(sum) < -1.0e-15) throw std::runtime_error("choldc : matrix not positive definite");
+                    if (val(sum) < 1.0e-15) sum = T(0.0);
+                    chol[size_t(i) * n + i] = mSqrt(sum);
+                }
+                else
+                    chol[size_t(i) * n + j] = std::fabs(val(chol[size_t(j) * n + j])) < 1.0e-15
+                                                  ? T(0.0) : sum / chol[size_t(j) * n + j];
+            }
+        // per step: dividend-adjusted forward factors, stds and drifts
+        const size_t ns = nSteps();
+        stds.resize(ns * n);
+        drifts.resize(ns * n);
+        ffs.resize(ns * n);
+        for (size_t i = 0; i < ns; ++i)
+        {
+            const double t1 = tl[i], t2 = tl[i + 1], dt = t2 - t1;
+            for (int a = 0; a < n; ++a)  // mcMdlMultiDisplaced.h:343-364
+            {
+                T divProd(1.0);
+                int d = int(std::lower_bound(m->divDates, m->divDates + m->nDiv, t1) - m->divDates);
+                while (d < m->nDiv && m->divDates[d] < t2)
+                {
+                    divProd = divProd * (1.0 - divs[size_t(d) * n + a]);
+                    ++d;
+                }
+                ffs[i * n + a] = divProd * exp(repo[a] * dt);
+                T& sd = stds[i * n + a];
+                T& dr = drifts[i * n + a];
+                switch (dyn[a])
+                {
+                case MD_LOG: sd = beta[a] * std::sqrt(dt); dr = -0.5 * sd * sd; break;
+                case MD_NORMAL: sd = alphas[a] * std::sqrt(dt); dr = T(0.0); break;
+                case MD_SUR: sd = beta[a] * std::sqrt(dt); dr = -0.5 * beta[a] * beta[a] * dt; break;
+                default: sd = -beta[a] * std::sqrt(dt); dr = -0.5 * beta[a] * beta[a] * dt; break;
+                }
+            }
+        }
+        // numeraires exp(r t) on the product dates (all of them ask for one); the forward
+        // factors of the samples (spot(t) = forward(t, t)) are exp(repo * 0) = 1
+        nums.resize(ptl.size());
+        for (size_t e = 0; e < ptl.size(); ++e) nums[e] = exp(disc * ptl[e]);
+    }
+
+    // generatePath (mcMdlMultiDisplaced.h:612-662): spots[e][a] on the product dates
+    void generatePath(const double* g, T* spotsOut) const
+    {
+        const int n = m->nA;
+        vector<T> s(spot.begin(), spot.end());
+        size_t idx = 0;
+        if (todayOn)
+        {
+            for (int a = 0; a < n; ++a) spotsOut[a] = s[a];
+            ++idx;
+        }
+        for (size_t i = 0; i < nSteps(); ++i)
+        {
+            const double* w = g + i * n;
+            for (int a = 0; a < n; ++a)
+            {
+                T cw(0.0);
+                for (int b = 0; b <= a; ++b) cw = cw + chol[size_t(a) * n + b] * w[b];
+                const T fwd = s[a] * ffs[i * n + a];
+                const T& sd = stds[i * n + a];
+                const T& dr = drifts[i * n + a];
+                switch (dyn[a])
+                {
+                case MD_LOG: s[a] = fwd * exp(dr + sd * cw); break;
+                case MD_NORMAL: s[a] = fwd + sd * cw; break;
+                case MD_SUR: s[a] = (fwd + alphas[a]) * exp(dr + sd * cw) - alphas[a]; break;
+                default: s[a] = (fwd - alphas[a]) * exp(dr + sd * cw) + alphas[a]; break;
+                }
+            }
+            for (int a = 0; a < n; ++a) spotsOut[idx * n + a] = s[a];
+            ++idx;
+        }
+    }
+};
+
+template <>
+double MdRun<double>::leafOf(double x) { return x; }
+template <>
+Var MdRun<Var>::leafOf(double x) { return leaf(x); }
+
+template <class T>
+T tmin(const T& a, double b);
+template <>
+double tmin(const double& a, double b) { return std::min(a, b); }
+template <>
+Var tmin(const Var& a, double b) { return un(std::min(a.v, b), a, a.v < b ? 1.0 : 0.0); }
+inline bool lessV(double a, double b) { return a < b; }
+inline bool lessV(const Var& a, const Var& b) { return a.v < b.v; }
+
+// Payoffs (mcPrdMulti.h:266-276 Baskets, 368-416 Autocall); spots [nEv][nA], nums [nEv].
+template <class T>
+void mPayoffsOf(const orc_mproduct& p, const T* sp, const vector<T>& nums, T* out)
+{
+    const int n = p.nA;
+    if (p.kind == 0)
+    {
+        T basket(0.0);
+        for (int a = 0; a < n; ++a) basket = basket + p.weights[a] * sp[a];
+        for (int k = 0; k < p.nK; ++k) out[k] = vmax(basket - p.strikes[k], 0.0) / nums[0];
+        return;
+    }
+    const double dt = p.maturity / p.periods;
+    const double smooth = std::max(p.smooth, kEps);
+    T alive(1.0), pay(0.0);
+    vector<T> perf(n);
+    auto worstOf = [&](int e) {
+        for (int a = 0; a < n; ++a) perf[a] = sp[size_t(e) * n + a] / p.refs[a];
+        size_t w = 0;
+        for (int a = 1; a < n; ++a)
+            if (lessV(perf[a], perf[w])) w = a;
+        return perf[w];
+    };
+    for (int e = 0; e < p.periods - 1; ++e)
+    {
+        const T worst = worstOf(e);
+        pay = pay + alive * p.cpn * dt / nums[e];
+        const T surv = alive * tmin(vmax((p.ko + smooth - worst) / 2 / smooth, 0.0), 1.0);
+        const T dead = alive - surv;
+        pay = pay + dead / nums[e];
+        alive = surv;
+    }
+    const int e = p.periods - 1;
+    const T worst = worstOf(e);
+    pay = pay + alive * p.cpn * dt / nums[e];
+    pay = pay + alive / nums[e];
+    pay = pay - alive * vmax(p.strike - worst, 0.0) / p.strike / nums[e];
+    out[0] = pay;
+}
+
+// Path loop for values (mcBase.h:267-308) and the tape-based risk (mcBase.h:427-532, 775-854).
+void mRun(const orc_mmodel& m, const orc_mproduct& p, int sobol, unsigned s1, unsigned s2, uint64_t nPath,
+          const double* weights, int mode /* 0 value, 1 aggregate risk, 2 multi risk */, double* paySum,
+          double* paySq, double* aggSum, double* riskSum)
+{
+    const int nPay = mPayoffs(p), n = m.nA;
+    const size_t nEv = mTimeline(p).size();
+    if (mode == 0)
+    {
+        MdRun<double> mr;
+        mr.allocate(m, p);
+        mr.putParams(false);
+        mr.init();
+        const int dim = int(mr.nSteps()) * n;
+        auto rng = makeRng(sobol, s1, s2, dim);
+        vector<double> g(dim), sp(nEv * n), pay(nPay);
+        for (uint64_t i = 0; i < nPath; ++i)
+        {
+            rng->nextG(g.data());
+            mr.generatePath(g.data(), sp.data());
+            mPayoffsOf(p, sp.data(), mr.nums, pay.data());
+            for (int k = 0; k < nPay; ++k)
+            {
+                paySum[k] += pay[k];
+                paySq[k] += pay[k] * pay[k];
+            }
+        }
+        return;
+    }
+    Tape tape;
+    gTape = &tape;
+    MdRun<Var> mr;
+    mr.allocate(m, p);
+    mr.putParams(true);
+    mr.init();
+    tape.mark = tape.nodes.size();
+    tape.width = mode == 2 ? nPay : 1;
+    tape.adj.assign(tape.mark * tape.width, 0.0);
+    const int dim = int(mr.nSteps()) * n;
+    auto rng = makeRng(sobol, s1, s2, dim);
+    vector<double> g(dim);
+    vector<Var> sp(nEv * n), pay(nPay);
+    for (uint64_t i = 0; i < nPath; ++i)
+    {
+        tape.nodes.resize(tape.mark);
+        rng->nextG(g.data());
+        mr.generatePath(g.data(), sp.data());
+        mPayoffsOf(p, sp.data(), mr.nums, pay.data());
+        for (int k = 0; k < nPay; ++k) paySum[k] += pay[k].v;
+        Var agg(0.0);
+        if (mode == 1)
+        {
+            for (int k = 0; k < nPay; ++k)
+                if (weights[k] != 0.0) agg = agg + pay[k] * weights[k];
+            *aggSum += agg.v;
+        }
+        tape.adj.resize(tape.nodes.size() * tape.width, 0.0);
+        if (mode == 2)
+        {
+            for (int k = 0; k < nPay; ++k)
+                if (pay[k].i >= 0) tape.adj[size_t(pay[k].i) * tape.width + k] += 1.0;
+        }
+        else if (agg.i >= 0)
+            tape.adj[size_t(agg.i)] += 1.0;
+        tape.sweep(tape.nodes.size(), tape.mark);
+        tape.adj.resize(tape.mark * tape.width);
+    }
+    tape.nodes.resize(tape.mark);
+    tape.sweep(tape.mark, 0);
+    for (size_t j = 0; j < mr.params.size(); ++j)
+        for (int w = 0; w < tape.width; ++w)
+            if (mr.params[j].i >= 0) riskSum[j * tape.width + w] += tape.adj[size_t(mr.params[j].i) * tape.width + w];
+    gTape = nullptr;
+}
+
+}  // namespace
+
 extern "C" {
 
 int orc_shapes(const orc_model* m, const orc_product* p, int* nPay, int* nParam, int* simDim)
@@ -1408,6 +1751,105 @@ int orc_fill(const double* x, int n, double maxDx, double minDx, const double* a
                         : fillData(vector<double>(x, x + n), maxDx, minDx);
     if (out) std::copy(f.begin(), f.end(), out);
     return int(f.size());
+}
+
+}  // extern "C"
+
+extern "C" {
+
+int orc_m_shapes(const orc_mmodel* m, const orc_mproduct* p, int* nPay, int* nParam, int* simDim)
+{
+    if (nPay) *nPay = mPayoffs(*p);
+    if (nParam) *nParam = int(mParams(*m));
+    MdRun<double> mr;
+    mr.allocate(*m, *p);
+    if (simDim) *simDim = int(mr.nSteps()) * m->nA;
+    return 0;
+}
+
+int orc_m_value(const orc_mmodel* m, const orc_mproduct* p, int sobol, int nPath, unsigned s1, unsigned s2,
+                double* values, double* stderrs)
+{
+    const int nPay = mPayoffs(*p);
+    vector<double> sum(nPay, 0.0), sq(nPay, 0.0);
+    try
+    {
+        mRun(*m, *p, sobol, s1, s2, uint64_t(nPath), nullptr, 0, sum.data(), sq.data(), nullptr, nullptr);
+    }
+    catch (const std::exception&)
+    {
+        return -1;
+    }
+    for (int k = 0; k < nPay; ++k)
+    {
+        values[k] = sum[k] / nPath;
+        if (stderrs) stderrs[k] = std::sqrt(std::max(0.0, sq[k] / nPath - values[k] * values[k]) / nPath);
+    }
+    return 0;
+}
+
+int orc_m_risk(const orc_mmodel* m, const orc_mproduct* p, int sobol, int nPath, unsigned s1, unsigned s2,
+               const double* weights, double* values, double* aggValue, double* risks)
+{
+    const int nPay = mPayoffs(*p);
+    const size_t nParam = mParams(*m);
+    vector<double> sum(nPay, 0.0), rk(nParam, 0.0);
+    double agg = 0.0;
+    try
+    {
+        mRun(*m, *p, sobol, s1, s2, uint64_t(nPath), weights, 1, sum.data(), nullptr, &agg, rk.data());
+    }
+    catch (const std::exception&)
+    {
+        return -1;
+    }
+    for (int k = 0; k < nPay; ++k) values[k] = sum[k] / nPath;
+    *aggValue = agg / nPath;
+    for (size_t j = 0; j < nParam; ++j) risks[j] = rk[j] / nPath;
+    return 0;
+}
+
+int orc_m_risk_multi(const orc_mmodel* m, const orc_mproduct* p, int sobol, int nPath, unsigned s1, unsigned s2,
+                     double* values, double* risks)
+{
+    const int nPay = mPayoffs(*p);
+    const size_t nParam = mParams(*m);
+    vector<double> sum(nPay, 0.0), rk(nParam * nPay, 0.0);
+    try
+    {
+        mRun(*m, *p, sobol, s1, s2, uint64_t(nPath), nullptr, 2, sum.data(), nullptr, nullptr, rk.data());
+    }
+    catch (const std::exception&)
+    {
+        return -1;
+    }
+    for (int k = 0; k < nPay; ++k) values[k] = sum[k] / nPath;
+    for (size_t j = 0; j < rk.size(); ++j) risks[j] = rk[j] / nPath;
+    return 0;
+}
+
+int orc_m_init(const orc_mmodel* m, const orc_mproduct* p, double* chol, double* stds, double* drifts, double* ffs,
+               double* alphas, int* dynamics, double* numeraires)
+{
+    MdRun<double> mr;
+    mr.allocate(*m, *p);
+    mr.putParams(false);
+    try
+    {
+        mr.init();
+    }
+    catch (const std::exception&)
+    {
+        return -1;
+    }
+    std::copy(mr.chol.begin(), mr.chol.end(), chol);
+    std::copy(mr.stds.begin(), mr.stds.end(), stds);
+    std::copy(mr.drifts.begin(), mr.drifts.end(), drifts);
+    std::copy(mr.ffs.begin(), mr.ffs.end(), ffs);
+    std::copy(mr.alphas.begin(), mr.alphas.end(), alphas);
+    std::copy(mr.dyn.begin(), mr.dyn.end(), dynamics);
+    std::copy(mr.nums.begin(), mr.nums.end(), numeraires);
+    return 0;
 }
 
 }  // extern "C"

@@ -112,6 +112,47 @@ int orc_superbucket(const orc_ivs* ivs, double spot, double maxDt, const orc_pro
                     unsigned seed2, int refSeedQuirk, double* value, double* delta, double* vega,
                     double* microbucket);
 
+/* Multiple correlated assets under displaced Black-Scholes dynamics with proportional
+ * dividends (mcMdlMultiDisplaced.h), and the multi-asset products (mcPrdMulti.h). */
+typedef struct {
+    int nA;                 /* assets */
+    double disc;            /* discount rate */
+    const double* spots;    /* [nA] */
+    const double* spreads;  /* [nA] repo spreads */
+    int nDiv;
+    const double* divDates; /* [nDiv] */
+    const double* divs;     /* [nDiv][nA] proportional dividends */
+    const double* atms;     /* [nA] */
+    const double* skews;    /* [nA] */
+    const double* correl;   /* [nA][nA]; the lower triangle is used */
+    double lambda;          /* used correl = lambda (1 - correl) + correl */
+} orc_mmodel;
+
+typedef struct {
+    int kind;               /* 0 = Baskets, 1 = Autocall */
+    int nA;
+    const double* weights;  /* Baskets [nA] */
+    double maturity;
+    int nK;
+    const double* strikes;  /* Baskets [nK] */
+    const double* refs;     /* Autocall [nA] */
+    int periods;
+    double ko, strike, cpn, smooth;
+} orc_mproduct;
+
+int orc_m_shapes(const orc_mmodel* m, const orc_mproduct* p, int* nPay, int* nParam, int* simDim);
+int orc_m_value(const orc_mmodel* m, const orc_mproduct* p, int sobol, int nPath, unsigned seed1,
+                unsigned seed2, double* values, double* stderrs);
+/* AADriskOne / AADriskAggregate (weights[nPay]) and AADriskMulti (risks[nParam * nPay]) */
+int orc_m_risk(const orc_mmodel* m, const orc_mproduct* p, int sobol, int nPath, unsigned seed1,
+               unsigned seed2, const double* weights, double* values, double* aggValue, double* risks);
+int orc_m_risk_multi(const orc_mmodel* m, const orc_mproduct* p, int sobol, int nPath, unsigned seed1,
+                     unsigned seed2, double* values, double* risks);
+/* Model quantities after init: chol[nA*nA], stds/drifts/ffs[nSteps*nA], alphas[nA],
+ * dynamics[nA] (0 lognormal, 1 normal, 2 surnormal, 3 subnormal), numeraires[nEv]. */
+int orc_m_init(const orc_mmodel* m, const orc_mproduct* p, double* chol, double* stds, double* drifts,
+               double* ffs, double* alphas, int* dynamics, double* numeraires);
+
 /* fillData(utility.h) for host-logic tests; returns count, fills out when non-NULL. */
 int orc_fill(const double* x, int n, double maxDx, double minDx, const double* add, int nAdd,
              double* out);

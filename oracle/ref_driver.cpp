@@ -55,6 +55,26 @@ EXPOSE(BsTimeline, BSD, std::vector<double>, myTimeline)
 EXPOSE(BsStds, BSD, std::vector<double>, myStds)
 EXPOSE(BsDrifts, BSD, std::vector<double>, myDrifts)
 EXPOSE(BsNums, BSD, std::vector<double>, myNumeraires)
+typedef MultiDisplaced<double> MdD;
+EXPOSE(MdTimeline, MdD, std::vector<double>, myTimeline)
+EXPOSE(MdChol, MdD, matrix<double>, myChol)
+EXPOSE(MdStds, MdD, matrix<double>, myStds)
+EXPOSE(MdDrifts, MdD, matrix<double>, myDrifts)
+EXPOSE(MdFfs, MdD, matrix<double>, myDynFwdFacts)
+EXPOSE(MdNums, MdD, std::vector<double>, myNumeraires)
+
+template <class M>
+static std::vector<double> flat(const M& m)
+{
+    return std::vector<double>(m.begin(), m.begin() + m.rows() * m.cols());
+}
+
+static std::vector<string> rdnames(std::istream& is, size_t n)
+{
+    std::vector<string> v(n);
+    for (auto& s : v) is >> s;
+    return v;
+}
 
 static std::vector<double> mrgState(const mrg32k3a& r)
 {
@@ -303,6 +323,50 @@ int main()
             auto strikes = rdv(std::cin, n);
             putEuropeans(mats, strikes, id);
         }
+        else if (cmd == "displaced")  // id nA names spots atms skews disc spreads nDiv divDates divs correl lambda
+        {
+            string id;
+            size_t nA, nD;
+            std::cin >> id >> nA;
+            auto names = rdnames(std::cin, nA);
+            auto spots = rdv(std::cin, nA), atms = rdv(std::cin, nA), skews = rdv(std::cin, nA);
+            double disc = rd(std::cin);
+            auto spreads = rdv(std::cin, nA);
+            std::cin >> nD;
+            auto divDates = rdv(std::cin, nD);
+            matrix<double> divs(nD, nA), correl(nA, nA);
+            for (size_t i = 0; i < nD; ++i)
+                for (size_t j = 0; j < nA; ++j) divs[i][j] = rd(std::cin);
+            for (size_t i = 0; i < nA; ++i)
+                for (size_t j = 0; j < nA; ++j) correl[i][j] = rd(std::cin);
+            double lambda = rd(std::cin);
+            putDisplaced(names, spots, atms, skews, disc, spreads, divDates, divs, correl, lambda, id);
+        }
+        else if (cmd == "baskets")  // id nA names weights maturity nK strikes
+        {
+            string id;
+            size_t nA, nK;
+            std::cin >> id >> nA;
+            auto names = rdnames(std::cin, nA);
+            auto w = rdv(std::cin, nA);
+            double mat = rd(std::cin);
+            std::cin >> nK;
+            auto k = rdv(std::cin, nK);
+            putBaskets(names, w, mat, k, id);
+        }
+        else if (cmd == "autocall")  // id nA names refs maturity periods ko strike cpn smooth
+        {
+            string id;
+            size_t nA;
+            int periods;
+            std::cin >> id >> nA;
+            auto names = rdnames(std::cin, nA);
+            auto refs = rdv(std::cin, nA);
+            double mat = rd(std::cin);
+            std::cin >> periods;
+            double ko = rd(std::cin), k = rd(std::cin), cpn = rd(std::cin), sm = rd(std::cin);
+            putAutocall(names, refs, mat, periods, ko, k, cpn, sm, id);
+        }
         else if (cmd == "labels")  // mid pid
         {
             string mid, pid;
@@ -323,6 +387,19 @@ int main()
                 put("common_steps", std::vector<double>(c.begin(), c.end()));
                 const auto& iv = d->*member(DupIv());
                 put("interp_vols", std::vector<double>(iv.begin(), iv.begin() + iv.rows() * iv.cols()));
+            }
+            if (auto* d = dynamic_cast<MultiDisplaced<double>*>(m.get()))
+            {
+                put("sim_timeline", d->*member(MdTimeline()));
+                put("md_chol", flat(d->*member(MdChol())));
+                put("md_stds", flat(d->*member(MdStds())));
+                put("md_drifts", flat(d->*member(MdDrifts())));
+                put("md_ffs", flat(d->*member(MdFfs())));
+                put("md_numeraires", d->*member(MdNums()));
+                put("md_alphas", d->alphas());
+                std::vector<double> dyn;
+                for (auto x : d->dynamics()) dyn.push_back(double(int(x)));
+                put("md_dynamics", dyn);
             }
             if (auto* b = dynamic_cast<BlackScholes<double>*>(m.get()))
             {

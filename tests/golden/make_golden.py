@@ -7,7 +7,7 @@ AADriskAggregate, AADriskMulti, bumpRisk, dupireCalib, dupireSuperbucket, the RN
 Every case records its inputs next to its outputs, so the fixtures are self-contained:
 the tests never need the reference.
 
-    python3 tests/golden/make_golden.py [rng host mc calib bump products]   # all when none named;
+    python3 tests/golden/make_golden.py [rng host mc calib bump products multi_asset]   # all when none named;
                                                                    # rebuilds the driver when missing
 """
 import json
@@ -367,6 +367,108 @@ def product_cases(models):
     return out
 
 
+def md_models_products():
+    """Multi-asset displaced model (mcMdlMultiDisplaced.h) and products (mcPrdMulti.h).  The four
+    assets of md4 take the four dynamics of the displacement rule: skew 0 (lognormal),
+    atm + 2 skew > 0 (surnormal), < 0 (subnormal), = 0 (normal)."""
+    models = {
+        "md4": dict(assets=["A", "B", "C", "D"], spots=[100.0, 50.0, 80.0, 120.0], atms=[0.2, 0.25, 0.15, 0.2],
+                    skews=[0.0, -0.05, -0.1, -0.1], disc=0.03, spreads=[0.01, 0.0, 0.02, -0.01],
+                    div_dates=[0.4, 1.2, 2.5],
+                    divs=[[0.02, 0.0, 0.01, 0.03], [0.01, 0.02, 0.0, 0.0], [0.02, 0.01, 0.01, 0.01]],
+                    correl=[[1.0, 0.5, 0.3, 0.2], [0.5, 1.0, 0.4, 0.1], [0.3, 0.4, 1.0, 0.25], [0.2, 0.1, 0.25, 1.0]],
+                    **{"lambda": 0.1}),
+        "md2": dict(assets=["X", "Y"], spots=[100.0, 100.0], atms=[0.2, 0.3], skews=[0.0, -0.05], disc=0.02,
+                    spreads=[0.0, 0.005], div_dates=[0.5], divs=[[0.02, 0.0]], correl=[[1.0, 0.6], [0.6, 1.0]],
+                    **{"lambda": 0.0}),
+    }
+    products = {
+        "bask4": dict(kind="baskets", assets=["A", "B", "C", "D"], weights=[0.25, 0.3, 0.2, 0.25], maturity=2.0,
+                      strikes=[70.0, 80.0, 86.0, 95.0, 105.0]),
+        "ac4": dict(kind="autocall", assets=["A", "B", "C", "D"], refs=[100.0, 50.0, 80.0, 120.0], maturity=3.0,
+                    periods=6, ko=1.0, strike=0.7, cpn=0.06, smooth=0.05),
+        "ac4_sharp": dict(kind="autocall", assets=["A", "B", "C", "D"], refs=[100.0, 50.0, 80.0, 120.0],
+                          maturity=2.0, periods=4, ko=1.05, strike=0.8, cpn=0.04, smooth=0.0),
+        "bask2": dict(kind="baskets", assets=["X", "Y"], weights=[0.5, 0.5], maturity=1.0, strikes=[100.0, 108.0]),
+        "ac2": dict(kind="autocall", assets=["X", "Y"], refs=[100.0, 100.0], maturity=1.0, periods=12, ko=1.02,
+                    strike=0.75, cpn=0.03, smooth=0.02),
+    }
+    return models, products
+
+
+def md_model_cmd(mid, m):
+    n = len(m["assets"])
+    divs = [x for row in m["divs"] for x in row]
+    corr = [x for row in m["correl"] for x in row]
+    return (f"displaced {mid} {n} {' '.join(m['assets'])} {fl(m['spots'])} {fl(m['atms'])} {fl(m['skews'])} "
+            f"{f(m['disc'])} {fl(m['spreads'])} {len(m['div_dates'])} {fl(m['div_dates'])} {fl(divs)} {fl(corr)} "
+            f"{f(m['lambda'])}")
+
+
+def md_product_cmd(pid, p):
+    n = len(p["assets"])
+    if p["kind"] == "baskets":
+        return (f"baskets {pid} {n} {' '.join(p['assets'])} {fl(p['weights'])} {f(p['maturity'])} "
+                f"{len(p['strikes'])} {fl(p['strikes'])}")
+    return (f"autocall {pid} {n} {' '.join(p['assets'])} {fl(p['refs'])} {f(p['maturity'])} {p['periods']} "
+            f"{f(p['ko'])} {f(p['strike'])} {f(p['cpn'])} {f(p['smooth'])}")
+
+
+def multi_asset_cases():
+    """value, AADriskOne, AADriskAggregate, AADriskMulti and bumpRisk of the multi-asset products
+    through the reference, with the model's initialised quantities (Cholesky factor, per-step
+    stds, drifts and dividend-adjusted forward factors, displacements, numeraires)."""
+    models, products = md_models_products()
+    cases = [("md4_bask4_sobol", "md4", "bask4", 1, 4096), ("md4_bask4_mrg", "md4", "bask4", 0, 4096),
+             ("md4_ac4_sobol", "md4", "ac4", 1, 2048), ("md4_ac4_mrg", "md4", "ac4", 0, 2048),
+             ("md4_ac4_sharp", "md4", "ac4_sharp", 1, 2048), ("md2_bask2_sobol", "md2", "bask2", 1, 2048),
+             ("md2_ac2_mrg", "md2", "ac2", 0, 2048)]
+    cmds = [md_model_cmd(mid, m) for mid, m in models.items()] + \
+           [md_product_cmd(pid, p) for pid, p in products.items()]
+    for (_, mid, pid, sob, n) in cases:
+        npay = len(products[pid]["strikes"]) if products[pid]["kind"] == "baskets" else 1
+        agg = [(k, 1.0 + 0.5 * k) for k in range(npay)]
+        cmds += [f"labels {mid} {pid}", f"value {mid} {pid} {num(sob, n)}", f"risk {mid} {pid} {num(sob, n)} 0",
+                 f"riskagg {mid} {pid} {num(sob, n)} {len(agg)} " + " ".join(f"{k} {f(w)}" for k, w in agg),
+                 f"riskmulti {mid} {pid} {num(sob, n)}", f"bump {mid} {pid} {num(sob, min(n, 512))}"]
+    res = run(cmds)
+    it = iter(res)
+    out = {"models": models, "products": products, "cases": []}
+    for (name, mid, pid, sob, n) in cases:
+        npay = len(products[pid]["strikes"]) if products[pid]["kind"] == "baskets" else 1
+        rec = dict(name=name, model=mid, product=pid, sobol=sob, npath=n, bump_npath=min(n, 512), seed1=12345,
+                   seed2=1234, agg_weights=[1.0 + 0.5 * k for k in range(npay)])
+        d = {}
+        while True:  # labels block: tags until md_dynamics
+            tag, v = next(it)
+            d[tag] = v
+            if tag == "md_dynamics":
+                break
+        rec["payoff_labels"], rec["param_labels"] = d["payoff_labels"], d["param_labels"]
+        for k in ("sim_timeline", "md_chol", "md_stds", "md_drifts", "md_ffs", "md_numeraires", "md_alphas",
+                  "md_dynamics"):
+            rec[k] = d[k]
+        rec["values"] = next(it)[1]
+        next(it)
+        next(it)
+        rec["risk_value"] = next(it)[1][0]
+        rec["risks"] = next(it)[1]
+        next(it)
+        next(it)
+        rec["agg_value"] = next(it)[1][0]
+        rec["agg_risks"] = next(it)[1]
+        next(it)
+        rec["multi_risks"] = next(it)[1]
+        next(it)
+        next(it)
+        next(it)
+        rec["bump_risks"] = next(it)[1]
+        next(it)
+        next(it)
+        out["cases"].append(rec)
+    return out
+
+
 def calib_cases():
     out = {}
     incl_spots, maxds, incl_times, maxdtv = W.superbucket_grid(60, 30)
@@ -426,7 +528,8 @@ def main():
     only = set(sys.argv[1:])
     for name, fn in [("rng", rng_cases), ("host", lambda: host_cases(models, products)),
                      ("mc", lambda: mc_cases(models, products)), ("calib", calib_cases),
-                     ("bump", lambda: bump_cases(models, products)), ("products", lambda: product_cases(models))]:
+                     ("bump", lambda: bump_cases(models, products)), ("products", lambda: product_cases(models)),
+                     ("multi_asset", multi_asset_cases)]:
         if only and name not in only:
             continue
         obj = fn()

@@ -148,6 +148,66 @@ class Engine:
         self._label_cache.pop(("p", id), None)
         return id
 
+    # ---- multi-asset store (store.h:75-94, 224-255) --------------------------------------
+    @staticmethod
+    def _names(assets):
+        arr = (ctypes.c_char_p * len(assets))(*[a.encode() for a in assets])
+        return arr
+
+    def putDisplaced(self, assets, spots, atms, skews, discRate, repoSpreads, divDates, divs, correl, lambda_, id):
+        """MultiDisplaced (mcMdlMultiDisplaced.h): divs [len(divDates)][nA], correl [nA][nA] (the lower
+        triangle is the model's)."""
+        n = len(assets)
+        sp, at, sk, rs = _arr(spots), _arr(atms), _arr(skews), _arr(repoSpreads)
+        dd = _arr(divDates) if len(divDates) else _arr([0.0])
+        dv = _arr(np.asarray(divs, dtype=float).reshape(-1)) if len(divDates) else _arr([0.0])
+        co = _arr(np.asarray(correl, dtype=float).reshape(-1))
+        if sp.size != n or at.size != n or sk.size != n or rs.size != n or co.size != n * n or \
+                (len(divDates) and dv.size != n * len(divDates)):
+            raise CfError(-1, "putDisplaced: inconsistent dimensions")
+        _check(lib().cf_put_displaced(self._h, n, self._names(assets), _p(sp), _p(at), _p(sk),
+                                      ctypes.c_double(discRate), _p(rs), len(divDates), _p(dd), _p(dv), _p(co),
+                                      ctypes.c_double(lambda_), id.encode()))
+        self._label_cache.pop(("m", id), None)
+        return id
+
+    def putBaskets(self, assets, weights, maturity, strikes, id):
+        w, k = _arr(weights), _arr(strikes)
+        if w.size != len(assets):
+            raise CfError(-1, "putBaskets: one weight per asset")
+        _check(lib().cf_put_baskets(self._h, len(assets), self._names(assets), _p(w), ctypes.c_double(maturity),
+                                    len(k), _p(k), id.encode()))
+        self._label_cache.pop(("p", id), None)
+        return id
+
+    def putAutocall(self, assets, refs, maturity, periods, ko, strike, cpn, smooth, id):
+        r = _arr(refs)
+        if r.size != len(assets):
+            raise CfError(-1, "putAutocall: one reference per asset")
+        _check(lib().cf_put_autocall(self._h, len(assets), self._names(assets), _p(r), ctypes.c_double(maturity),
+                                     int(periods), ctypes.c_double(ko), ctypes.c_double(strike),
+                                     ctypes.c_double(cpn), ctypes.c_double(smooth), id.encode()))
+        self._label_cache.pop(("p", id), None)
+        return id
+
+    def mdState(self, modelId, productId):
+        """Initialised multi-asset model: dict(s0, chol, stds, drifts, ffs, alphas, numeraires, dynamics)."""
+        cnt = ctypes.c_int()
+        _check(lib().cf_md_state(self._h, modelId.encode(), productId.encode(), None, 0, ctypes.byref(cnt), None))
+        npay, npar, dim = self.shapes(modelId, productId)
+        d = np.zeros(cnt.value)
+        # the asset count: the model's "spot <asset>" parameters
+        nA = sum(1 for l in self.parameterLabels(modelId) if l.startswith("spot "))
+        dyn = np.zeros(nA, dtype=np.int32)
+        _check(lib().cf_md_state(self._h, modelId.encode(), productId.encode(), _p(d), cnt.value, ctypes.byref(cnt),
+                                 dyn.ctypes.data_as(ctypes.POINTER(ctypes.c_int))))
+        ns = dim // nA
+        o = [0, nA, nA + nA * nA, nA + nA * nA + ns * nA, nA + nA * nA + 2 * ns * nA, nA + nA * nA + 3 * ns * nA,
+             2 * nA + nA * nA + 3 * ns * nA]
+        return dict(s0=d[o[0]:o[1]], chol=d[o[1]:o[2]].reshape(nA, nA), stds=d[o[2]:o[3]].reshape(ns, nA),
+                    drifts=d[o[3]:o[4]].reshape(ns, nA), ffs=d[o[4]:o[5]].reshape(ns, nA), alphas=d[o[5]:o[6]],
+                    numeraires=d[o[6]:], dynamics=dyn)
+
     def _labels(self, fn, key, kind):
         got = self._label_cache.get((kind, key))
         if got is None:

@@ -27,12 +27,6 @@ namespace {
 
 constexpr double kBump = 1.0e-08;  // main.h:346
 
-double& model_param(ModelDesc& m, int i)
-{
-    if (i == 0) return m.spot;
-    if (m.kind == MODEL_BS) return i == 1 ? m.vol : i == 2 ? m.rate : m.div;
-    return m.vols[size_t(i - 1)];  // spot-major, the order of the parameter labels
-}
 
 }  // namespace
 
@@ -53,7 +47,7 @@ int bump_risk_reprice(Context& c, const std::string& mid, const std::string& pid
     ModelDesc mb = m0;
     for (int i = 0; i < nParam; ++i)
     {
-        double& x = model_param(mb, i);
+        double& x = mb.param(i);
         const double keep = x;
         x += kBump;
         Plan bp;

@@ -4,12 +4,46 @@
 // per-step model coefficients, the event map from simulation steps to product dates, and
 // the product's constants.  Kernels never see strings, virtual calls or host pointers.
 #pragma once
+#include <cuda_runtime.h>
+
 #include <cstdint>
 
 namespace cf {
 
-enum ModelKind : int { MODEL_BS = 0, MODEL_DUPIRE = 1 };
-enum ProductKind : int { PROD_EUROPEAN = 0, PROD_UOC = 1, PROD_EUROPEANS = 2, PROD_CONTINGENT = 3 };
+enum ModelKind : int { MODEL_BS = 0, MODEL_DUPIRE = 1, MODEL_MULTI = 2 };
+enum ProductKind : int
+{
+    PROD_EUROPEAN = 0,
+    PROD_UOC = 1,
+    PROD_EUROPEANS = 2,
+    PROD_CONTINGENT = 3,
+    PROD_BASKETS = 4,
+    PROD_AUTOCALL = 5
+};
+// Dynamics of one asset of the multi-asset displaced model (mcMdlMultiDisplaced.h:31-37).
+enum MdDynamics : int { MD_LOGNORMAL = 0, MD_NORMAL = 1, MD_SURNORMAL = 2, MD_SUBNORMAL = 3 };
+
+// Derived quantities of the multi-asset model, one array (the kernels' inputs, and the
+// quantities whose path adjoints the risk kernel sums): initial spots [nA], Cholesky factor
+// [nA][nA] (lower triangle used), per step stds, drifts and dividend-adjusted forward factors
+// [nSteps][nA] each, displacements [nA], numeraires of the product dates [nEv].
+struct MdLayout
+{
+    int s0, chol, std_, drift, ff, alpha, num, total;
+};
+__host__ __device__ inline MdLayout md_layout(int nA, int nSteps, int nEv)
+{
+    MdLayout L;
+    L.s0 = 0;
+    L.chol = nA;
+    L.std_ = L.chol + nA * nA;
+    L.drift = L.std_ + nSteps * nA;
+    L.ff = L.drift + nSteps * nA;
+    L.alpha = L.ff + nSteps * nA;
+    L.num = L.alpha + nA;
+    L.total = L.num + nEv;
+    return L;
+}
 enum RngKind : int { RNG_MRG = 0, RNG_SOBOL = 1 };
 
 // Error bits written by kernels into McParams::err (host turns them into CF_E_DEVICE).
@@ -141,6 +175,17 @@ struct McParams
     int nodeShiftF;
     long long nodeSlabOffset;
     const float* invnF;   // [512][4] piecewise-cubic inverse normal of the launch's generator
+
+    // multi-asset displaced model (mcMdlMultiDisplaced.h) with Baskets / Autocall
+    // (mcPrdMulti.h); nSteps is the number of time steps, the Gaussians per path nSteps * nA
+    int nA;
+    int prodKind;         // PROD_BASKETS or PROD_AUTOCALL
+    const int* mdDyn;     // [nA] MdDynamics
+    const double* mdD;    // derived quantities (md_layout), FP64 and FP32 copies
+    const float* mdF;
+    const double* mdAssetD;  // [nA] basket weights, or autocall reference levels
+    const float* mdAssetF;
+    double acKo, acStrike, acCpn, acDt, acSmooth;  // autocall: KO level, put strike, coupon, period, smoothing
 
     // Dupire raw inputs for bumped revaluation (bumpRisk): vols [nS][nT] spot-major, and per
     // step sqrt(dt) and the time weight t of interp_lin, so that a bumped node's sqrt(dt) sigma

@@ -42,12 +42,6 @@ int cuda_fail(cudaError_t e, const char* what)
                 std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-#define CF_CUDA(call)                                         \
-    do                                                        \
-    {                                                         \
-        cudaError_t e_ = (call);                              \
-        if (e_ != cudaSuccess) return cuda_fail(e_, #call);   \
-    } while (0)
 
 // ------------------------------------------------------------------------------------
 // Device buffers
@@ -169,6 +163,35 @@ void ProductDesc::build()
         labels = {l1 + " up and out " + fmt2(barrier) + " monitoring freq " + fmt2(freq) + " smooth " + fmt2(smooth),
                   l1};
     }
+    else if (kind == PROD_BASKETS)
+    {
+        // mcPrdMulti.h:201-221: the maturity, numeraire and spot(T) of every asset
+        timeline = {maturity};
+        fwdMat = {maturity};
+        discMat = {NAN};
+        needNum = {1};
+        for (double k : strikes) labels.push_back("basket strike " + fmt2(k));
+        kflat = strikes;
+    }
+    else if (kind == PROD_AUTOCALL)
+    {
+        // mcPrdMulti.h:297-324: periods equally spaced dates (accumulated as the reference does)
+        double t = 0.0;
+        const double dt = maturity / periods;
+        for (int k = 0; k < periods; ++k)
+        {
+            t += dt;
+            timeline.push_back(t);
+            fwdMat.push_back(t);
+            discMat.push_back(NAN);
+            needNum.push_back(1);
+        }
+        constexpr double kEps = 1.0e-08;  // utility.h:9
+        labels = {"autocall strike " + std::to_string(int(100 * strike + kEps)) + " KO " +
+                  std::to_string(int(100 * ko + kEps)) + " CPN " + std::to_string(int(100 * cpn + kEps)) + " " +
+                  std::to_string(periods) + " periods of " + std::to_string(int(12 * maturity / periods + kEps)) +
+                  "m"};
+    }
     else
     {
         std::map<double, std::vector<double>> opts;
@@ -193,6 +216,22 @@ void ProductDesc::build()
 void ModelDesc::build()
 {
     labels.clear();
+    if (kind == MODEL_MULTI)
+    {
+        // mcMdlMultiDisplaced.h:146-209
+        const size_t n = assets.size();
+        labels.push_back("disc rate");
+        for (size_t a = 0; a < n; ++a) labels.push_back("spot " + assets[a]);
+        for (size_t a = 0; a < n; ++a) labels.push_back("repo spread " + assets[a]);
+        for (double d : divDates)
+            for (size_t a = 0; a < n; ++a) labels.push_back("div " + assets[a] + " " + fmt2(d));
+        for (size_t a = 0; a < n; ++a) labels.push_back("ATM " + assets[a]);
+        for (size_t a = 0; a < n; ++a) labels.push_back("skew " + assets[a]);
+        for (size_t i = 1; i < n; ++i)
+            for (size_t j = 0; j < i; ++j) labels.push_back("correl " + assets[i] + " " + assets[j]);
+        labels.push_back("lambda");
+        return;
+    }
     labels.push_back("spot");
     if (kind == MODEL_BS)
     {
@@ -206,7 +245,56 @@ void ModelDesc::build()
                 labels.push_back("lvol " + fmt2(spots[i]) + " " + fmt2(times[j]));
 }
 
-int ModelDesc::numParams() const { return kind == MODEL_BS ? 4 : 1 + int(spots.size() * times.size()); }
+int ModelDesc::numParams() const
+{
+    if (kind == MODEL_MULTI)
+    {
+        const int n = int(assets.size());
+        return 1 + 2 * n + n * int(divDates.size()) + 2 * n + n * (n - 1) / 2 + 1;
+    }
+    return kind == MODEL_BS ? 4 : 1 + int(spots.size() * times.size());
+}
+
+double& ModelDesc::param(int i)
+{
+    if (kind != MODEL_MULTI)
+    {
+        if (i == 0) return spot;
+        if (kind == MODEL_BS) return i == 1 ? vol : i == 2 ? rate : div;
+        return vols[size_t(i - 1)];  // spot-major, the order of the parameter labels
+    }
+    const int n = int(assets.size()), nD = int(divDates.size());
+    if (i == 0) return disc;
+    --i;
+    if (i < n) return aSpots[i];
+    i -= n;
+    if (i < n) return spreads[i];
+    i -= n;
+    if (i < n * nD) return divs[size_t(i)];
+    i -= n * nD;
+    if (i < n) return atms[i];
+    i -= n;
+    if (i < n) return skews[i];
+    i -= n;
+    for (int r = 1; r < n; ++r)
+        for (int c = 0; c < r; ++c)
+            if (i-- == 0) return correl[size_t(r) * n + c];
+    return lambda;
+}
+
+namespace {
+const std::vector<std::string> kDefaultAsset = {"spot"};  // mcBase.h:125, 160
+}
+
+const std::vector<std::string>& ModelDesc::assetNames() const
+{
+    return kind == MODEL_MULTI ? assets : kDefaultAsset;
+}
+
+const std::vector<std::string>& ProductDesc::assetNames() const
+{
+    return kind == PROD_BASKETS || kind == PROD_AUTOCALL ? assets : kDefaultAsset;
+}
 
 // ------------------------------------------------------------------------------------
 // Plan: the flat device tables of one (model, product) pair.
@@ -238,6 +326,10 @@ std::vector<float> to_f(const std::vector<T>& v)
 int Context::buildPlan(const ModelDesc& m, const ProductDesc& pd, Plan& plan)
 {
     // plan arrives freshly constructed (getPlan makes a new one per build)
+    if (m.assetNames() != pd.assetNames()) return fail(CF_E_ARG, "Model and product are not compatible");  // mcBase.h:253-259
+    if (m.kind == MODEL_MULTI) return buildPlanMd(m, pd, plan);
+    if (pd.kind == PROD_BASKETS || pd.kind == PROD_AUTOCALL)
+        return fail(CF_E_UNSUPPORTED, "Baskets and Autocall products run on the multi-asset model");
     plan.model = m.kind;
     plan.prod = pd.kind;
     plan.nPay = int(pd.labels.size());
@@ -619,6 +711,7 @@ int Context::enqueue(Slot& slot, Plan& plan, const cf_num_param& num, bool risk,
 {
     if (num.numPath <= 0) return fail(CF_E_ARG, "numPath must be positive");
     if (firstPath < 0 || firstPath % 64) return fail(CF_E_ARG, "firstPath must be a non-negative multiple of 64");
+    if (plan.model == MODEL_MULTI) return enqueueMd(slot, plan, num, risk, weights, firstPath);
     const bool sobol = num.useSobol != 0;
     if (sobol && !plan.sobolOk)
         return fail(CF_E_SHAPE, "Sobol dimension " + std::to_string(plan.nSteps) + " exceeds the " +
@@ -744,6 +837,17 @@ size_t Context::footprint(const Plan& plan, const cf_num_param& num, bool risk) 
 {
     const bool sobol = num.useSobol != 0, fp32 = num.precision == CF_FP32;
     const int NP = sobol ? 1 : 2;
+    if (plan.model == MODEL_MULTI)
+    {
+        // multi-asset: per thread the Gaussians, the spots and the notionals of the reverse
+        // sweep; at most 4 resident blocks of 128 threads per SM (the kernels are register-heavy)
+        const long long needed = sobol ? (num.numPath / 32 + 1) * 32 : (num.numPath + 1) / 2;
+        const long long threads = std::min<long long>(needed, (long long)numSMs * 4 * 128);
+        const size_t dim = size_t(plan.nSteps) * plan.base.nA;
+        size_t b = size_t(plan.mdTotal + 2 * plan.nPay + 2) * 16 + 4096;
+        if (risk) b += (dim + NP * dim + NP * size_t(plan.nEv)) * size_t(threads) * (fp32 ? 4 : 8);
+        return b;
+    }
     // resident threads of the launch (the grid of enqueue), bounded by the occupancy limit
     McParams p = plan.base;
     p.nRisk = risk ? plan.nParam : 0;
@@ -788,6 +892,22 @@ int Context::fetch(Slot& slot, double* values, double* stderrs, double* aggregat
     const long long* acc = static_cast<const long long*>(slot.hostAcc.ptr);
     const int e = *reinterpret_cast<const int*>(acc + 2 * size_t(p.nAcc));
     if (e) return fail(CF_E_DEVICE, "kernel error flag " + std::to_string(e));
+    if (slot.plan->model == MODEL_MULTI && slot.risk && risks)
+    {
+        // path-averaged adjoints of the derived quantities -> parameter risks through the
+        // Jacobian of the model's initialisation
+        const Plan& pl = *slot.plan;
+        std::vector<double> der(size_t(p.nRisk));
+        results_from_acc(acc, p.nRisk, p.nPay, p.nPath, values, stderrs, aggregate, der.data());
+        for (int j = 0; j < pl.nParam; ++j) risks[j] = 0.0;
+        for (int d = 0; d < p.nRisk; ++d)
+            if (der[d] != 0.0)
+            {
+                const double* row = &pl.mdJac[size_t(d) * pl.nParam];
+                for (int j = 0; j < pl.nParam; ++j) risks[j] += der[d] * row[j];
+            }
+        return CF_OK;
+    }
     results_from_acc(acc, p.nRisk, p.nPay, p.nPath, values, stderrs, aggregate, slot.risk ? risks : nullptr);
     return CF_OK;
 }
@@ -983,6 +1103,115 @@ int cf_put_europeans(cf_context* ctx, const double* maturities, const double* st
     return CF_OK;
 }
 
+static int read_names(int n, const char* const* names, std::vector<std::string>& out)
+{
+    out.clear();
+    if (n < 1 || !names) return fail(CF_E_ARG, "no assets");
+    for (int i = 0; i < n; ++i)
+    {
+        if (!names[i] || !*names[i]) return fail(CF_E_ARG, "empty asset name");
+        out.emplace_back(names[i]);
+    }
+    return CF_OK;
+}
+
+int cf_put_displaced(cf_context* ctx, int nA, const char* const* assets, const double* spots, const double* atms,
+                     const double* skews, double discRate, const double* repoSpreads, int nDiv,
+                     const double* divDates, const double* divs, const double* correl, double lambda, const char* id)
+{
+    CF_CTX();
+    if (check_id(id)) return CF_E_ARG;
+    ModelDesc m;
+    m.kind = MODEL_MULTI;
+    if (read_names(nA, assets, m.assets)) return CF_E_ARG;
+    if (nA > 16) return fail(CF_E_SHAPE, "putDisplaced: at most 16 assets");
+    if (!spots || !atms || !skews || !repoSpreads || !correl || nDiv < 0 || (nDiv > 0 && (!divDates || !divs)))
+        return fail(CF_E_ARG, "putDisplaced: missing inputs");
+    for (int d = 1; d < nDiv; ++d)
+        if (!(divDates[d] > divDates[d - 1])) return fail(CF_E_ARG, "putDisplaced: dividend dates must increase");
+    m.disc = discRate;
+    m.lambda = lambda;
+    m.aSpots.assign(spots, spots + nA);
+    m.atms.assign(atms, atms + nA);
+    m.skews.assign(skews, skews + nA);
+    m.spreads.assign(repoSpreads, repoSpreads + nA);
+    if (nDiv > 0)
+    {
+        m.divDates.assign(divDates, divDates + nDiv);
+        m.divs.assign(divs, divs + size_t(nDiv) * nA);
+    }
+    m.correl.assign(correl, correl + size_t(nA) * nA);
+    m.version = ++ctx->c.versionCounter;
+    m.build();
+    ctx->c.models[id] = std::move(m);
+    return CF_OK;
+}
+
+int cf_put_baskets(cf_context* ctx, int nA, const char* const* assets, const double* weights, double maturity, int nK,
+                   const double* strikes, const char* id)
+{
+    CF_CTX();
+    if (check_id(id)) return CF_E_ARG;
+    ProductDesc p;
+    p.kind = PROD_BASKETS;
+    if (read_names(nA, assets, p.assets)) return CF_E_ARG;
+    if (!(maturity > 0)) return fail(CF_E_ARG, "putBaskets: maturity must be positive");
+    if (!weights || !strikes || nK < 1) return fail(CF_E_ARG, "putBaskets: weights and strikes required");
+    p.weights.assign(weights, weights + nA);
+    p.maturity = maturity;
+    p.strikes.assign(strikes, strikes + nK);
+    p.version = ++ctx->c.versionCounter;
+    p.build();
+    ctx->c.products[id] = std::move(p);
+    return CF_OK;
+}
+
+int cf_put_autocall(cf_context* ctx, int nA, const char* const* assets, const double* refs, double maturity, int periods,
+                    double ko, double strike, double cpn, double smooth, const char* id)
+{
+    CF_CTX();
+    if (check_id(id)) return CF_E_ARG;
+    ProductDesc p;
+    p.kind = PROD_AUTOCALL;
+    if (read_names(nA, assets, p.assets)) return CF_E_ARG;
+    if (!refs) return fail(CF_E_ARG, "putAutocall: one reference level per asset");
+    if (!(maturity > 0) || periods < 1) return fail(CF_E_ARG, "putAutocall: positive maturity and periods");
+    p.refs.assign(refs, refs + nA);
+    p.maturity = maturity;
+    p.periods = periods;
+    p.ko = ko;
+    p.strike = strike;
+    p.cpn = cpn;
+    p.smooth = smooth;
+    p.version = ++ctx->c.versionCounter;
+    p.build();
+    ctx->c.products[id] = std::move(p);
+    return CF_OK;
+}
+
+int cf_md_state(cf_context* ctx, const char* modelId, const char* productId, double* derived, int capacity, int* count,
+                int* dynamics)
+{
+    CF_CTX();
+    Plan* plan;
+    int rc = ctx->c.getPlan(modelId ? modelId : "", productId ? productId : "", plan);
+    if (rc) return rc;
+    if (plan->model != MODEL_MULTI) return fail(CF_E_ARG, "not a multi-asset model");
+    if (count) *count = plan->mdTotal;
+    if (derived)
+    {
+        if (capacity < plan->mdTotal) return fail(CF_E_ARG, "cf_md_state: buffer too small");
+        std::memcpy(derived, plan->mdDerived.data(), size_t(plan->mdTotal) * 8);
+    }
+    if (dynamics)
+    {
+        std::vector<int> dyn(plan->base.nA);
+        CF_CUDA(cudaMemcpy(dyn.data(), plan->base.mdDyn, dyn.size() * 4, cudaMemcpyDeviceToHost));
+        std::memcpy(dynamics, dyn.data(), dyn.size() * 4);
+    }
+    return CF_OK;
+}
+
 static int write_labels(const std::vector<std::string>& l, char* buf, size_t size, int* count, size_t* needed)
 {
     std::string s;
@@ -1023,7 +1252,7 @@ int cf_shapes(cf_context* ctx, const char* modelId, const char* productId, int* 
     if (rc) return rc;
     if (nPay) *nPay = plan->nPay;
     if (nParam) *nParam = plan->nParam;
-    if (simDim) *simDim = plan->nSteps;
+    if (simDim) *simDim = plan->model == MODEL_MULTI ? plan->nSteps * plan->base.nA : plan->nSteps;
     return CF_OK;
 }
 
@@ -1140,6 +1369,10 @@ int cf_enqueue_shard(cf_context* ctx, const char* modelId, const char* productId
     Plan* plan;
     int rc = ctx->c.getPlan(modelId ? modelId : "", productId ? productId : "", plan);
     if (rc) return rc;
+    // a shard's raw accumulators carry parameter adjoints for the single-asset models; the
+    // multi-asset model's are adjoints of its derived quantities (mapped in fetch)
+    if (risk && plan->model == MODEL_MULTI)
+        return fail(CF_E_UNSUPPORTED, "sharded risk runs cover the Black-Scholes and Dupire models");
     std::vector<double> w;
     if (risk && !weights)
     {

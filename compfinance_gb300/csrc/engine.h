@@ -15,6 +15,13 @@ namespace cf {
 
 int fail(int code, const std::string& msg);
 int cuda_fail(cudaError_t e, const char* what);
+// return the failure of a CUDA call as a status (CF_E_CUDA / CF_E_NOMEM with the message)
+#define CF_CUDA(call)                                       \
+    do                                                      \
+    {                                                       \
+        cudaError_t e_ = (call);                            \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+    } while (0)
 double fix_value_host(long long hi, long long lo);
 void results_from_acc(const long long* acc, int nRisk, int nPay, long long nPath, double* values, double* stderrs,
                       double* aggregate, double* risks);
@@ -31,7 +38,8 @@ struct DevBuf
     ~DevBuf() { release(); }
 };
 
-// A model of the store (store.h:38-73): Black-Scholes or Dupire.
+// A model of the store (store.h:38-94): Black-Scholes, Dupire, or multiple correlated
+// displaced assets.
 struct ModelDesc
 {
     int kind = MODEL_BS;
@@ -39,27 +47,43 @@ struct ModelDesc
     bool qSpot = false;
     std::vector<double> spots, times, vols;  // Dupire, vols spot-major
     double maxDt = 0.25;
+    // multi-asset displaced (mcMdlMultiDisplaced.h): names, discount rate, per asset spot,
+    // repo spread, ATM vol and skew, dividends [nDiv][nA] on divDates, correl [nA][nA] (its
+    // lower triangle is the model's), and the correl shift lambda
+    std::vector<std::string> assets;
+    double disc = 0, lambda = 0;
+    std::vector<double> aSpots, spreads, divDates, divs, atms, skews, correl;
     std::vector<std::string> labels;
     unsigned long long version = 0;
     void build();
     int numParams() const;
+    double& param(int i);  // parameter i in label order (bumpRisk)
+    const std::vector<std::string>& assetNames() const;
 };
 
-// A product of the store (store.h:128-205): European, up-and-out, Europeans.
+// A product of the store (store.h:128-255): European, up-and-out, Europeans, contingent
+// bond, Baskets, Autocall.
 struct ProductDesc
 {
     int kind = PROD_EUROPEAN;
     double strike = 0, exercise = 0, settlement = 0, barrier = 0, maturity = 0, freq = 0, smooth = 0;
     double coupon = 0;  // contingent bond
     int callPut = 0;
-    std::vector<double> mats, strikes;  // Europeans input pairs
+    std::vector<double> mats, strikes;  // Europeans input pairs; Baskets strikes
+    // multi-asset: asset names, basket weights or autocall references, autocall periods, KO, coupon
+    std::vector<std::string> assets;
+    std::vector<double> weights, refs;
+    int periods = 0;
+    double ko = 0, cpn = 0;
     // derived
     std::vector<double> timeline, fwdMat, discMat, kflat, libEnd;  // libEnd: libor end per date, NaN if none
     std::vector<int> needNum, payOff;
     std::vector<std::string> labels;
     unsigned long long version = 0;
     void build();
+    const std::vector<std::string>& assetNames() const;
 };
+
 
 // The device tables of one (model, product) pair.
 struct Plan
@@ -73,6 +97,10 @@ struct Plan
     std::vector<int> evAtStep;
     DevBuf tables;
     McParams base;
+    // multi-asset model: derived quantities (md_layout) and their Jacobian to the model
+    // parameters, [total][nParam], from the host-side adjoint of the model's initialisation
+    std::vector<double> mdDerived, mdJac;
+    int mdTotal = 0;
 };
 
 // Pinned host memory (results are copied into it asynchronously).
@@ -134,6 +162,9 @@ struct Context
     ~Context();
     int getPlan(const std::string& mid, const std::string& pid, Plan*& out);
     int buildPlan(const ModelDesc& m, const ProductDesc& pd, Plan& plan);
+    int buildPlanMd(const ModelDesc& m, const ProductDesc& pd, Plan& plan);  // multi_asset.cpp
+    int enqueueMd(Slot& slot, Plan& plan, const cf_num_param& num, bool risk, const double* weights,
+                  long long firstPath);
     const ProductDesc* productOf(const Plan& plan) const;
     int enqueue(Slot& slot, Plan& plan, const cf_num_param& num, bool risk, const double* weights,
                 long long firstPath = 0);

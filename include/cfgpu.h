@@ -72,15 +72,41 @@ int cf_put_dupire(cf_context* ctx, double spot, const double* spots, int nSpots,
 int cf_put_european(cf_context* ctx, double strike, double exerciseDate, double settlementDate,
                     const char* id);
 /* putBarrier, store.h:144-163 (smooth <= 0 is replaced by 1e-8 as in the reference) */
+int cf_put_barrier(cf_context* ctx, double strike, double barrier, double maturity, double monitorFreq,
+                   double smooth, int callPut, const char* id);
 /* putContingent, store.h:165-180 (ContingentBond, mcPrd.h:404-574): pays (libor(Ti, Ti+1) +
  * coupon) x (Ti+1 - Ti) at Ti+1 when the spot rose over the period (a digital smoothed over
  * +-smooth x the first spot; smooth <= 0: a sharp digital), plus the redemption at maturity. */
 int cf_put_contingent(cf_context* ctx, double coupon, double maturity, double payFreq, double smooth, const char* id);
-int cf_put_barrier(cf_context* ctx, double strike, double barrier, double maturity, double monitorFreq,
-                   double smooth, int callPut, const char* id);
 /* putEuropeans, store.h:184-205 (maturities in increasing order) */
 int cf_put_europeans(cf_context* ctx, const double* maturities, const double* strikes, int n,
                      const char* id);
+/* putDisplaced, store.h:75-94 (MultiDisplaced, mcMdlMultiDisplaced.h:28-717): nA correlated
+ * assets (1 to 16, names without blanks) with spots, ATM vols and skews (the displacement rule
+ * of mcMdlMultiDisplaced.h:418-444), a discount rate, repo spreads, proportional dividends
+ * divs[nDiv][nA] on divDates (increasing), a correlation [nA][nA] whose lower triangle is the
+ * model's, and lambda (used correlation = lambda (1 - correl) + correl).  The checks of
+ * xPutDisplaced (xlExport.cpp:158-176). */
+int cf_put_displaced(cf_context* ctx, int nA, const char* const* assets, const double* spots, const double* atms,
+                     const double* skews, double discRate, const double* repoSpreads, int nDiv,
+                     const double* divDates, const double* divs, const double* correl, double lambda,
+                     const char* id);
+/* putBaskets, store.h:224-237 (Baskets, mcPrdMulti.h:181-277): max(sum_a w_a S_a(T) - K, 0)
+ * per strike. */
+int cf_put_baskets(cf_context* ctx, int nA, const char* const* assets, const double* weights, double maturity,
+                   int nK, const double* strikes, const char* id);
+/* putAutocall, store.h:239-255 (Autocall, mcPrdMulti.h:279-439): periods equal periods to
+ * maturity on the worst performance S_a / ref_a; coupon cpn per year while alive, smoothed
+ * knock-out at ko (smoothing max(smooth, 1e-8)), redemption less a put struck at strike. */
+int cf_put_autocall(cf_context* ctx, int nA, const char* const* assets, const double* refs, double maturity,
+                    int periods, double ko, double strike, double cpn, double smooth, const char* id);
+/* The initialised multi-asset model of a (model, product) pair (init, mcMdlMultiDisplaced.h:
+ * 407-566), in this order: initial spots [nA], Cholesky factor [nA][nA], stds, drifts and
+ * dividend-adjusted forward factors [nSteps][nA] each, displacements [nA], numeraires
+ * [nDates]; *count their number (derived == NULL: the count only); dynamics[nA] (when not
+ * NULL): 0 lognormal, 1 normal, 2 surnormal, 3 subnormal. */
+int cf_md_state(cf_context* ctx, const char* modelId, const char* productId, double* derived, int capacity,
+                int* count, int* dynamics);
 
 /* Product::payoffLabels (mcBase.h:137) and Model::parameterLabels (mcBase.h:194): labels
  * written '\n'-separated into buf (NUL-terminated); *count receives their number.  With

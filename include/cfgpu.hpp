@@ -175,6 +175,56 @@ inline void putEuropeans(const std::vector<double>& maturities, const std::vecto
                   "putEuropeans()");
 }
 
+namespace detail {
+inline std::vector<const char*> cnames(const std::vector<std::string>& v)
+{
+    std::vector<const char*> out;
+    for (const auto& x : v) out.push_back(x.c_str());
+    return out;
+}
+}  // namespace detail
+
+// store.h:75-94 (MultiDisplaced): same arguments in the same order as the reference
+inline void putDisplaced(const std::vector<std::string>& assets, const std::vector<double>& spots,
+                         const std::vector<double>& atms, const std::vector<double>& skews, const double& discRate,
+                         const std::vector<double>& repoSpreads, const std::vector<double>& divDates,
+                         const matrix<double>& divs, const matrix<double>& correl, const double& lambda,
+                         const std::string& store)
+{
+    const size_t n = assets.size();
+    if (!n || spots.size() != n || atms.size() != n || skews.size() != n || repoSpreads.size() != n ||
+        divs.rows() != divDates.size() || (divDates.size() && divs.cols() != n) || correl.rows() != n ||
+        correl.cols() != n)
+        throw std::runtime_error("putDisplaced() : inconsistent dimensions");
+    const auto names = detail::cnames(assets);
+    detail::check(cf_put_displaced(detail::ctx(), int(n), names.data(), spots.data(), atms.data(), skews.data(),
+                                   discRate, repoSpreads.data(), int(divDates.size()), divDates.data(),
+                                   divs.v.data(), correl.v.data(), lambda, store.c_str()),
+                  "putDisplaced()");
+}
+
+// store.h:224-237
+inline void putBaskets(const std::vector<std::string>& assets, const std::vector<double>& weights, double maturity,
+                       const std::vector<double> strikes, const std::string& store)
+{
+    if (weights.size() != assets.size()) throw std::runtime_error("putBaskets() : one weight per asset");
+    const auto names = detail::cnames(assets);
+    detail::check(cf_put_baskets(detail::ctx(), int(assets.size()), names.data(), weights.data(), maturity,
+                                 int(strikes.size()), strikes.data(), store.c_str()),
+                  "putBaskets()");
+}
+
+// store.h:239-255
+inline void putAutocall(const std::vector<std::string>& assets, const std::vector<double>& refs, double maturity,
+                        int periods, double ko, double strike, double cpn, double smooth, const std::string& store)
+{
+    if (refs.size() != assets.size()) throw std::runtime_error("putAutocall() : one reference per asset");
+    const auto names = detail::cnames(assets);
+    detail::check(cf_put_autocall(detail::ctx(), int(assets.size()), names.data(), refs.data(), maturity, periods,
+                                  ko, strike, cpn, smooth, store.c_str()),
+                  "putAutocall()");
+}
+
 inline std::vector<std::string> getPayoffLabels(const std::string& productId)
 {
     return detail::labels(cf_payoff_labels, productId, "getPayoffLabels()");

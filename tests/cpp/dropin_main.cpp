@@ -60,7 +60,33 @@ int main()
     {
         notDupire = std::string(e.what()).find("not a Dupire") != std::string::npos;
     }
-    std::printf("{\"value\": [%.17g, %.17g], \"risk_value\": %.17g, \"risk0\": %.17g, \"risk5\": %.17g,"
+    // multi-asset: store.h:75-94 and 224-255 with the reference's argument order
+    matrix<double> divs(1, 2), correl(2, 2);
+    divs[0][0] = 0.02;
+    divs[0][1] = 0.0;
+    correl[0][0] = correl[1][1] = 1.0;
+    correl[0][1] = correl[1][0] = 0.6;
+    putDisplaced({"X", "Y"}, {100.0, 100.0}, {0.2, 0.3}, {0.0, -0.05}, 0.02, {0.0, 0.005}, {0.5}, divs, correl, 0.0,
+                 "md");
+    putAutocall({"X", "Y"}, {100.0, 100.0}, 1.0, 12, 1.02, 0.75, 0.03, 0.02, "ac");
+    putBaskets({"X", "Y"}, {0.5, 0.5}, 1.0, {100.0, 108.0}, "bk");
+    const auto ac = AADriskOne("md", "ac", sob);
+    const auto bk = AADriskMulti("md", "bk", num);
+    bool incompatible = false;
+    try
+    {
+        value("dupire", "ac", num);
+    }
+    catch (const std::runtime_error& e)
+    {
+        incompatible = std::string(e.what()).find("not compatible") != std::string::npos;
+    }
+    std::printf("{\"md\": {\"ac_value\": %.17g, \"ac_risks\": [%.17g, %.17g, %.17g], \"ac_nparams\": %zu, "
+                "\"ac_label\": \"%s\", \"param12\": \"%s\", \"bk_shape\": [%zu, %zu], \"bk_00\": %.17g, "
+                "\"incompatible\": %d},\n",
+                ac.riskPayoffValue, ac.risks[0], ac.risks[1], ac.risks[11], ac.risks.size(), ac.payoffIds[0].c_str(),
+                ac.paramIds[11].c_str(), bk.risks.rows(), bk.risks.cols(), bk.risks[0][0], incompatible ? 1 : 0);
+    std::printf(" \"value\": [%.17g, %.17g], \"risk_value\": %.17g, \"risk0\": %.17g, \"risk5\": %.17g,"
                 " \"nparams\": %zu, \"bs\": [%.17g, %.17g, %.17g, %.17g, %.17g], \"multi_shape\": [%zu, %zu],"
                 " \"multi00\": %.17g, \"label0\": \"%s\", \"threw\": %d, \"dupire\": [%.17g, %.17g, %.17g],"
                 " \"vega_shape\": [%zu, %zu], \"not_dupire\": %d, \"bump_shape\": [%zu, %zu], \"bump50\": %.17g}\n",

@@ -41,4 +41,16 @@ def test_cpp_dropin_program(tmp_path):
     # bumpRisk (main.h:316-359) in the RiskReports layout
     br = eng.bumpRisk("d", "u", NumericalParam(numPath=1 << 14))
     assert out["bump_shape"] == [201, 2] and out["bump50"] == br["risks"][50, 0]
+    # multi-asset store entries (store.h:75-94, 224-255) and the compatibility check
+    md = out["md"]
+    eng.putDisplaced(["X", "Y"], [100.0, 100.0], [0.2, 0.3], [0.0, -0.05], 0.02, [0.0, 0.005], [0.5], [[0.02, 0.0]],
+                     [[1.0, 0.6], [0.6, 1.0]], 0.0, "md")
+    eng.putAutocall(["X", "Y"], [100.0, 100.0], 1.0, 12, 1.02, 0.75, 0.03, 0.02, "ac")
+    eng.putBaskets(["X", "Y"], [0.5, 0.5], 1.0, [100.0, 108.0], "bk")
+    a = eng.AADriskOne("md", "ac", NumericalParam(useSobol=True, numPath=1 << 14))
+    assert md["ac_value"] == a["riskPayoffValue"] and md["ac_nparams"] == 13
+    assert md["ac_risks"] == [a["risks"][0], a["risks"][1], a["risks"][11]]
+    assert md["ac_label"] == a["payoffIds"][0] and md["param12"] == "correl Y X"
+    b = eng.AADriskMulti("md", "bk", NumericalParam(numPath=1 << 14))
+    assert md["bk_shape"] == [13, 2] and md["bk_00"] == b["risks"][0, 0] and md["incompatible"] == 1
     eng.close()

@@ -134,6 +134,45 @@ def cpu_baseline(seconds=12.0, threads=None):
             "sample": f"{n} paths of the same workload (FP64, hand-written adjoint), {dt:.2f} s"}
 
 
+def multi_asset_leg(eng, npath=1 << 20):
+    """The four-asset displaced model (one asset per dynamics, dividends, lambda-shifted
+    correlation): AADriskOne of the 6-period autocall (1 payoff) and of the 5-strike basket (the
+    first strike), 36 parameters, Sobol paths, FP32 and FP64 path arithmetic (wall clock,
+    synchronous calls after a warm-up)."""
+    from compfinance_gb300 import NumericalParam
+    mid, ac, bk = W.put_md4(eng)
+    out = {"paths": npath, "assets": len(W.MD4["assets"]), "params": eng.shapes(mid, ac)[1]}
+    for name, pid in (("autocall", ac), ("basket", bk)):
+        rec = {}
+        for prec in ("fp32", "fp64"):
+            num = NumericalParam(useSobol=True, numPath=npath, precision=prec)
+            eng.AADriskOne(mid, pid, num)
+            t0 = time.perf_counter()
+            r = eng.AADriskOne(mid, pid, num)
+            dt = time.perf_counter() - t0
+            rec[prec] = {"risk_s": dt, "paths_per_s": npath / dt, "value": r["riskPayoffValue"]}
+        out[name] = rec
+    return out
+
+
+def cpu_multi_asset(seconds=4.0):
+    """The oracle's tape-based AADriskOne of the four-asset autocall, one thread, on a bounded
+    sample (the reference's own procedure: a tape per path)."""
+    import oracle as O
+    m = O.MModel(dict(W.MD4, **{"lambda": W.MD4["lam"]}))
+    p = O.MProduct(dict(kind="autocall", assets=W.MD4["assets"], **W.MD4_AUTOCALL))
+    n = 1024
+    while True:
+        t0 = time.perf_counter()
+        O.m_risk(m, p, 1, n, [1.0])
+        dt = time.perf_counter() - t0
+        if dt > seconds / 4 or n >= 1 << 20:
+            break
+        n *= 2
+    return {"value": n / dt, "unit": "paths/s", "cores": 1, "kind": "port",
+            "sample": f"{n} Sobol paths of the four-asset autocall AADriskOne (FP64 tape), {dt:.2f} s"}
+
+
 def serving_leg(eng, n, seed):
     """Mixed request stream (seeded Poisson arrivals at 2,000 req/s; 40% BS values, 40% Dupire
     barrier risks of 2^16-2^20 paths on 20x10..120x60 grids with 12..520 steps, 20% European
@@ -448,10 +487,13 @@ def main():
         out["grid_sweep"] = grid_sweep(eng, stream, flush, npath)
         out["superbucket"] = superbucket_leg(eng)
         out["bump_risk"] = bump_leg(eng)
+        out["multi_asset"] = multi_asset_leg(eng)
     if not args.no_serving:
         out["serving"] = serving_leg(eng, args.serve_requests, seed=2026 + rank)
     if rank == 0 and not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline()
+        if "multi_asset" in out:
+            out["multi_asset"]["cpu_baseline"] = cpu_multi_asset()
     if rank == 0:
         print(json.dumps(out))
     eng.close()

@@ -164,3 +164,95 @@ def serving_stream(n=10000, rate=2000.0, seed=2026):
             out.append(dict(t=t[i], kind="multi", model=f"dup{s0:g}_{g[0]}x{g[1]}m", product=f"port{s0:g}_{npay}",
                             paths=1 << 16, sobol=True))
     return out
+
+
+# ---------------------------------------------------------------------------------------
+# Portfolio risk run (AADriskMulti of the superbucket portfolio on a synthetic Dupire surface)
+# for timing and profiling:
+#     python -m compfinance_gb300.workloads multi [GRID=60x30] [PATHS=1048576] [REPS=1] [fp32|fp64]
+# ---------------------------------------------------------------------------------------
+def run_multi(grid=(60, 30), paths=1 << 20, reps=1, precision="fp32", device=0):
+    """Times `reps` AADriskMulti calls (200 payoffs x (1 + nS nT) parameters, 36 monthly steps,
+    Sobol paths) after one warm-up call; returns seconds per call."""
+    import time
+    from compfinance_gb300 import Engine, NumericalParam
+    eng = Engine(device)
+    mats, strikes = superbucket_portfolio(10, 20)
+    eng.putEuropeans(mats, strikes, "port")
+    s, t, v = dupire_surface(*grid)
+    eng.putDupire(100.0, s, t, v, 1.0 / 12.0, "dup")
+    num = NumericalParam(useSobol=True, numPath=int(paths), precision=precision)
+    eng.AADriskMulti("dup", "port", num)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        eng.AADriskMulti("dup", "port", num)
+    dt = (time.perf_counter() - t0) / max(1, reps)
+    eng.close()
+    return dt
+
+
+# ---------------------------------------------------------------------------------------
+# Multi-asset workload (mcMdlMultiDisplaced.h, mcPrdMulti.h): four correlated assets, one per
+# dynamics of the displacement rule (lognormal, surnormal, subnormal, normal), with dividends;
+# a 6-period autocall and a 5-strike basket on them.
+# ---------------------------------------------------------------------------------------
+MD4 = dict(assets=["A", "B", "C", "D"], spots=[100.0, 50.0, 80.0, 120.0], atms=[0.2, 0.25, 0.15, 0.2],
+           skews=[0.0, -0.05, -0.1, -0.1], disc=0.03, spreads=[0.01, 0.0, 0.02, -0.01], div_dates=[0.4, 1.2, 2.5],
+           divs=[[0.02, 0.0, 0.01, 0.03], [0.01, 0.02, 0.0, 0.0], [0.02, 0.01, 0.01, 0.01]],
+           correl=[[1.0, 0.5, 0.3, 0.2], [0.5, 1.0, 0.4, 0.1], [0.3, 0.4, 1.0, 0.25], [0.2, 0.1, 0.25, 1.0]],
+           lam=0.1)
+MD4_AUTOCALL = dict(refs=[100.0, 50.0, 80.0, 120.0], maturity=3.0, periods=6, ko=1.0, strike=0.7, cpn=0.06,
+                    smooth=0.05)
+MD4_BASKET = dict(weights=[0.25, 0.3, 0.2, 0.25], maturity=2.0, strikes=[70.0, 80.0, 86.0, 95.0, 105.0])
+
+
+def put_md4(eng, mid="md4", ac="md4_ac", bk="md4_bk"):
+    m = MD4
+    eng.putDisplaced(m["assets"], m["spots"], m["atms"], m["skews"], m["disc"], m["spreads"], m["div_dates"],
+                     m["divs"], m["correl"], m["lam"], mid)
+    a = MD4_AUTOCALL
+    eng.putAutocall(m["assets"], a["refs"], a["maturity"], a["periods"], a["ko"], a["strike"], a["cpn"], a["smooth"],
+                    ac)
+    b = MD4_BASKET
+    eng.putBaskets(m["assets"], b["weights"], b["maturity"], b["strikes"], bk)
+    return mid, ac, bk
+
+
+def run_md(product="autocall", paths=1 << 20, reps=1, precision="fp32", risk=True, device=0):
+    """Times `reps` AADriskOne (risk) or value calls of the four-asset autocall or basket after one
+    warm-up call (Sobol paths); returns seconds per call."""
+    import time
+    from compfinance_gb300 import Engine, NumericalParam
+    eng = Engine(device)
+    mid, ac, bk = put_md4(eng)
+    pid = ac if product == "autocall" else bk
+    num = NumericalParam(useSobol=True, numPath=int(paths), precision=precision)
+    call = (lambda: eng.AADriskOne(mid, pid, num)) if risk else (lambda: eng.value(mid, pid, num))
+    call()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        call()
+    dt = (time.perf_counter() - t0) / max(1, reps)
+    eng.close()
+    return dt
+
+
+if __name__ == "__main__":
+    import sys
+    a = sys.argv[1:]
+    if a and a[0] in ("autocall", "basket"):
+        n = int(a[1]) if len(a) > 1 else 1 << 20
+        r = int(a[2]) if len(a) > 2 else 1
+        prec = a[3] if len(a) > 3 else "fp32"
+        sec = run_md(a[0], n, r, prec)
+        print(f"AADriskOne 4-asset {a[0]} {prec} {n} paths: {1e3 * sec:.3f} ms per call, {n / sec:.4g} paths/s")
+        raise SystemExit(0)
+    if not a or a[0] != "multi":
+        raise SystemExit("usage: python -m compfinance_gb300.workloads multi [GRID] [PATHS] [REPS] [fp32|fp64]\n"
+                         "       python -m compfinance_gb300.workloads autocall|basket [PATHS] [REPS] [fp32|fp64]")
+    g = tuple(int(x) for x in (a[1] if len(a) > 1 else "60x30").split("x"))
+    n = int(a[2]) if len(a) > 2 else 1 << 20
+    r = int(a[3]) if len(a) > 3 else 1
+    prec = a[4] if len(a) > 4 else "fp32"
+    sec = run_multi(g, n, r, prec)
+    print(f"AADriskMulti {g[0]}x{g[1]} {prec} {n} paths: {1e3 * sec:.3f} ms per call, {n / sec:.4g} paths/s")

@@ -215,6 +215,15 @@ void ProductDesc::build()
 
 void ModelDesc::build()
 {
+    labels_.clear();
+    labelsReady_ = false;
+}
+
+const std::vector<std::string>& ModelDesc::labels() const
+{
+    if (labelsReady_) return labels_;
+    labelsReady_ = true;
+    std::vector<std::string>& labels = labels_;
     labels.clear();
     if (kind == MODEL_MULTI)
     {
@@ -230,7 +239,7 @@ void ModelDesc::build()
         for (size_t i = 1; i < n; ++i)
             for (size_t j = 0; j < i; ++j) labels.push_back("correl " + assets[i] + " " + assets[j]);
         labels.push_back("lambda");
-        return;
+        return labels_;
     }
     labels.push_back("spot");
     if (kind == MODEL_BS)
@@ -240,9 +249,17 @@ void ModelDesc::build()
         labels.push_back("div");
     }
     else
+    {
+        std::vector<std::string> ft(times.size());
+        for (size_t j = 0; j < times.size(); ++j) ft[j] = " " + fmt2(times[j]);
+        labels.reserve(1 + spots.size() * times.size());
         for (size_t i = 0; i < spots.size(); ++i)
-            for (size_t j = 0; j < times.size(); ++j)
-                labels.push_back("lvol " + fmt2(spots[i]) + " " + fmt2(times[j]));
+        {
+            const std::string fs = "lvol " + fmt2(spots[i]);
+            for (size_t j = 0; j < times.size(); ++j) labels.push_back(fs + ft[j]);
+        }
+    }
+    return labels_;
 }
 
 int ModelDesc::numParams() const
@@ -1241,7 +1258,7 @@ int cf_parameter_labels(cf_context* ctx, const char* modelId, char* buf, size_t 
     CF_CTX();
     auto it = ctx->c.models.find(modelId ? modelId : "");
     if (it == ctx->c.models.end()) return fail(CF_E_NOTFOUND, "model not found");
-    return write_labels(it->second.labels, buf, size, count, needed);
+    return write_labels(it->second.labels(), buf, size, count, needed);
 }
 
 int cf_shapes(cf_context* ctx, const char* modelId, const char* productId, int* nPay, int* nParam, int* simDim)

@@ -53,12 +53,18 @@ struct ModelDesc
     std::vector<std::string> assets;
     double disc = 0, lambda = 0;
     std::vector<double> aSpots, spreads, divDates, divs, atms, skews, correl;
-    std::vector<std::string> labels;
     unsigned long long version = 0;
     void build();
+    // parameter labels, formatted on first request (a 60x30 grid has 1801: formatting them on
+    // every putDupire would cost more than lowering the plan)
+    const std::vector<std::string>& labels() const;
     int numParams() const;
     double& param(int i);  // parameter i in label order (bumpRisk)
     const std::vector<std::string>& assetNames() const;
+
+private:
+    mutable std::vector<std::string> labels_;
+    mutable bool labelsReady_ = false;
 };
 
 // A product of the store (store.h:128-255): European, up-and-out, Europeans, contingent

@@ -2,7 +2,9 @@
 // -ffp-contract=off so the double arithmetic rounds exactly like the reference's.
 #include "host_math.h"
 
+#include <charconv>
 #include <cstdio>
+#include <system_error>
 #include <iterator>
 
 namespace cf {
@@ -43,11 +45,17 @@ double interp_lin(const double* x, size_t n, const double* y, double x0)
     return y[k] + (y[k + 1] - y[k]) * t;
 }
 
+// "%.2f" (correctly rounded, as printf; to_chars avoids the locale and format parsing)
 std::string fmt2(double x)
 {
-    char b[64];
-    std::snprintf(b, sizeof b, "%.2f", x);
-    return b;
+    char b[400];
+    const auto r = std::to_chars(b, b + sizeof b, x, std::chars_format::fixed, 2);
+    if (r.ec != std::errc())
+    {
+        std::snprintf(b, sizeof b, "%.2f", x);
+        return b;
+    }
+    return std::string(b, r.ptr);
 }
 
 namespace {

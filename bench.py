@@ -193,6 +193,18 @@ def serving_leg(eng, n, seed):
     served = stats["pathStepsDone"] / makespan
     batch_all = bstats["pathStepsDone"] / bmakespan
     batch = steps / t_seq
+    # the same requests at arrival rates that offer 80% and 90% of the batch capacity (arrival
+    # times scaled): p99 latency with the server under that load
+    load = []
+    for frac in (0.8, 0.9):
+        rate = frac * n / bmakespan
+        scaled = [dict(r, t=r["t"] * 2000.0 / rate) for r in stream]
+        lstats, lmakespan, _, _ = run_stream(eng, scaled, slots=8, budget=64 << 30)
+        load.append({"offered_over_batch": frac, "arrival_rate_req_s": rate,
+                     "completed": lstats["completed"], "failed": lstats["failed"],
+                     "p50_ms": lstats["p50Ms"], "p99_ms": lstats["p99Ms"], "mean_ms": lstats["meanMs"],
+                     "makespan_s": lmakespan,
+                     "served_over_batch": lstats["pathStepsDone"] / lmakespan / batch_all})
     return {"requests": n, "arrival_rate_req_s": 2000.0, "slots": 8, "hbm_budget_gb": 64,
             "completed": stats["completed"], "failed": stats["failed"], "rejected": stats["rejected"],
             "p50_ms": stats["p50Ms"], "p99_ms": stats["p99Ms"], "mean_ms": stats["meanMs"],
@@ -200,7 +212,7 @@ def serving_leg(eng, n, seed):
             "batch_makespan_s": bmakespan, "batch_path_steps_per_s": batch_all, "served_over_batch": served / batch_all,
             "one_at_a_time_s": t_seq, "one_at_a_time_path_steps_per_s": batch,
             "served_over_one_at_a_time": served / batch, "max_in_flight": stats["maxInFlight"],
-            "peak_footprint_gb": stats["peakFootprint"] / 2**30}
+            "peak_footprint_gb": stats["peakFootprint"] / 2**30, "load_sweep": load}
 
 
 def grid_sweep(eng, stream, flush, npath):
@@ -475,7 +487,12 @@ def main():
                      "frac": achieved / peak_fp32, "traffic": traffic,
                      "peak_source": "152 SM x 128 FP32 lanes x 2 x sm_max_mhz of MEASURED_PEAKS.json "
                                     "(no tensor-core or HBM bound applies)",
-                     "flops_per_path_step": FLOPS_PER_PATH_STEP},
+                     "flops_per_path_step": FLOPS_PER_PATH_STEP,
+                     # the same launch against the HBM roofline: its measured DRAM bytes (the
+                     # reverse-sweep scratch) over the launch time, of the measured copy bandwidth
+                     "hbm": ({"achieved_gbs": traffic / per_step / 1e9, "peak_gbs": pk.get("hbm_gbs"),
+                              "frac": traffic / per_step / 1e9 / pk["hbm_gbs"]}
+                             if traffic and pk.get("hbm_gbs") else None)},
         "e2e": {"value": world * npath / e2e_t, "unit": "paths/s", "h2d_bytes_per_step": (h1 - h0) // ke,
                 "d2h_bytes_per_step": (d1 - d0) // ke},
         "gpu_launches": launches,

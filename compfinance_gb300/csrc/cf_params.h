@@ -207,9 +207,17 @@ struct McLaunch
 int launch_mc(const McLaunch& l, const McParams& p, void* stream);   // returns cudaError_t
 int mc_smem_bytes(const McLaunch& l, const McParams& p, int stageY, size_t* bytes);
 int mc_occupancy(const McLaunch& l, size_t smem, int* blocksPerSM);
-int mc_scratch_fields(const McLaunch& l);   // reverse-sweep scratch fields of a risk launch
-// Bytes of a risk launch's scratch buffer: the fields [field][point][thread] for grid*128
-// threads, then (dupire_risk32) one int64 node slab per block.  Sets p.nodeSlabOffset.
+// dupire_risk32 keeps the reverse-sweep scratch of its last R32_RING unit rounds (a live path
+// may wait up to two rounds before its sweep); round r uses slot r mod R32_RING, so a launch
+// of fewer rounds needs only as many slots as it has rounds.
+constexpr int R32_RING = 3;
+// Unit rounds of a launch of `threads` threads over nPath paths (every thread runs the same
+// number of rounds).
+long long mc_rounds(const McLaunch& l, long long nPath, long long threads);
+// Reverse-sweep scratch fields of a risk launch of `rounds` unit rounds.
+int mc_scratch_fields(const McLaunch& l, long long rounds);
+// Bytes of a risk launch's scratch buffer: p.scratchFields fields [field][point][thread] for
+// grid*128 threads, then (dupire_risk32) one int64 node slab per block.  Sets p.nodeSlabOffset.
 size_t mc_scratch_bytes(const McLaunch& l, McParams& p, long long grid);
 // Whether a (model, product, precision, mode) launch of this plan runs dupire_risk32
 // (CF_FAST32=0 in the environment selects the generic kernel instead).

@@ -823,13 +823,14 @@ int Context::enqueue(Slot& slot, Plan& plan, const cf_num_param& num, bool risk,
     l.block = 128;
     if (risk)
     {
-        p.scratchFields = mc_scratch_fields(l);
         // kernels index the scratch with 32-bit offsets: keep fields*(steps+1)*threads < 2^31
-        const long long perThread = (long long)p.scratchFields * (plan.nSteps + 1);
+        // (sized for the full ring, the most fields a launch can need)
+        const long long perThread = (long long)mc_scratch_fields(l, R32_RING) * (plan.nSteps + 1);
         const long long maxThreads = ((1LL << 31) - 1) / perThread;
         if (grid * 128 > maxThreads) grid = std::max(1LL, maxThreads / 128);
         l.grid = int(grid);
         p.scratchThreads = grid * 128;
+        p.scratchFields = mc_scratch_fields(l, mc_rounds(l, p.nPath, grid * 128));
         const size_t bytes = mc_scratch_bytes(l, p, grid);
         if ((rc = slot.scratch.ensure(bytes))) return rc;
         p.scratch = slot.scratch.ptr;
@@ -886,7 +887,7 @@ size_t Context::footprint(const Plan& plan, const cf_num_param& num, bool risk) 
                size_t(plan.nPay + plan.nEv) * size_t(plan.nParam) * 16 + size_t(plan.nPay) * size_t(plan.nParam) * 8 +
                size_t(plan.nPay + plan.nEv) * 96 + 8192;
     }
-    const int fields = plan.prod == PROD_EUROPEANS ? 1 + 3 * NP : mc_scratch_fields(l);
+    const int fields = plan.prod == PROD_EUROPEANS ? 1 + 3 * NP : mc_scratch_fields(l, mc_rounds(l, num.numPath, threads));
     size_t b = size_t(plan.nParam + 2 * plan.nPay + 2) * 16 + size_t(plan.nPay) * 12 + 4096;
     if (risk) b += size_t(fields) * size_t(plan.nSteps + 1) * size_t(threads) * (fp32 ? 4 : 8);
     if (risk && l.fast) b += size_t((threads + 127) / 128) * size_t(plan.base.nS) * size_t(plan.base.nT) * 8 + 256;

@@ -11,16 +11,20 @@
 //     spot.  The forward itself uses the quantised weight, so the reverse sweep replays
 //     exactly the operations of the forward.
 //  2. compaction: paths whose adjoint seed is zero (knocked out, or out of the money at
-//     maturity) contribute nothing to any risk; the block lists the others.
-//  3. reverse: each listed path is swept back from maturity to today by one thread, with no
-//     block barrier inside the sweep.  The adjoint of each local-vol value the step used is
+//     maturity) contribute nothing to any risk; the block appends the others to a
+//     first-in-first-out list of pending paths.  The scratch is a ring of R32_RING round
+//     slots, so a listed path may wait up to two rounds for its sweep.
+//  3. reverse: while 128 paths are pending, the block sweeps a chunk of 128 (one path per
+//     thread, every thread busy); a partial chunk runs only when the oldest pending paths'
+//     slot is about to be rewritten, and once at the end.  Each listed path is swept back
+//     from maturity to today by one thread, with no block barrier inside the sweep.  The adjoint of each local-vol value the step used is
 //     split over its two spot knots and, with the step's time weights, over its two time
 //     columns, and each of the (up to) four parts is rounded once to an integer in units of
 //     2^-nodeShiftF and added (native 32-bit shared atomics) to an int32 slab of the
 //     local-vol nodes.  The host picks nodeShiftF so that no slab word can overflow within
-//     one unit round; after each round the slab is moved into a block-private int64 slab in
-//     global memory (each word owned by one thread), which is added to the accumulators
-//     once, at the end.  Each contribution is rounded once, so every sum is independent of
+//     256 paths; after each chunk (at most 128 paths) the slab is moved into a block-private
+//     int64 slab in global memory (each word owned by one thread), which is added to the
+//     accumulators once, at the end.  Each contribution is rounded once, so every sum is independent of
 //     how paths are grouped into warps, blocks and launches.
 #include <cuda_runtime.h>
 
@@ -43,12 +47,14 @@ constexpr float T_MAX = 1.0f - 1.0f / 4194304.0f;  // t + 2 stays below 3
 // Contributions with |adjoint| >= AV_MAX go exactly to the global accumulators instead of
 // the int32 slab (the host's choice of nodeShiftF assumes this bound).
 constexpr float AV_MAX = 512.0f;
+// pending-path list: a power of two above the most it holds (127 left over + 2 RB new)
+constexpr int LIST_CAP = 512;
 
 __host__ __device__ inline size_t a16(size_t x) { return (x + 15) & ~size_t(15); }
 
 struct R32Layout
 {
-    size_t slab, node, xs, ir, bucket, listIdx, listAx, listAl, cnt, stepc, invn, base, total;
+    size_t slab, node, xs, ir, bucket, listIdx, cnt, stepc, invn, base, total;
 };
 
 __host__ __device__ inline R32Layout r32_layout(int rng, const McParams& p)
@@ -57,7 +63,7 @@ __host__ __device__ inline R32Layout r32_layout(int rng, const McParams& p)
     size_t off = 0;
     L.slab = off;
     off += a16(size_t(4 + 2 * p.nPay + 2) * 16);
-    L.node = off;  // int32 local-vol node slab of the current unit round
+    L.node = off;  // int32 local-vol node slab of the current chunk
     off += a16(size_t(p.nS) * p.nT * 4);
     L.xs = off;
     off += a16(size_t(p.nS + 2) * 4);
@@ -65,12 +71,8 @@ __host__ __device__ inline R32Layout r32_layout(int rng, const McParams& p)
     off += a16(size_t(p.nS + 1) * 8);
     L.bucket = off;
     off += a16(size_t(p.nBucketsF) * 4);
-    L.listIdx = off;
-    off += a16(size_t(2 * RB) * 4);
-    L.listAx = off;
-    off += a16(size_t(2 * RB) * 4);
-    L.listAl = off;
-    off += a16(size_t(2 * RB) * 4);
+    L.listIdx = off;  // (ring slot << 8) | (thread << 1) | path of the pair
+    off += a16(size_t(LIST_CAP) * 2);
     L.cnt = off;
     off += 16;
     L.stepc = off;  // (colA, colB, weight A, weight B in units of 2^-nodeShiftF) per step
@@ -96,9 +98,7 @@ __global__ void __launch_bounds__(RB, 8) dupire_risk32(const McParams p)
     float* sXs = reinterpret_cast<float*>(smem + L.xs);
     float2* sIr = reinterpret_cast<float2*>(smem + L.ir);
     int* sBucket = reinterpret_cast<int*>(smem + L.bucket);
-    int* listIdx = reinterpret_cast<int*>(smem + L.listIdx);
-    float* listAx = reinterpret_cast<float*>(smem + L.listAx);
-    float* listAl = reinterpret_cast<float*>(smem + L.listAl);
+    unsigned short* listIdx = reinterpret_cast<unsigned short*>(smem + L.listIdx);
     int* cnt = reinterpret_cast<int*>(smem + L.cnt);
     int4* stepc = reinterpret_cast<int4*>(smem + L.stepc);
     float4* sInvn = reinterpret_cast<float4*>(smem + L.invn);
@@ -139,12 +139,18 @@ __global__ void __launch_bounds__(RB, 8) dupire_risk32(const McParams p)
     const float bX0 = p.bX0F, bInvW = p.bInvWF;
     const int nB = p.nBucketsF;
 
-    // scratch [field][point][thread], 32-bit offsets (the host keeps it below 2^31 elements)
+    // scratch [ring slot][field][point][thread], 32-bit offsets (the host keeps it below 2^31
+    // elements).  Point nSteps of a path's step-word field holds its adjoint seed, and point
+    // nSteps of its survival-factor field (barrier) the seed of the survival factor.
     const int Ti = int(gridDim.x) * RB;
     const int rowStride = (nSteps + 1) * Ti;
-    float* scr = reinterpret_cast<float*>(p.scratch);
     constexpr int F_G = 0, F_W = 1, F_B = 1 + NP, F_S = 1 + 2 * NP;
+    constexpr int NF = UOC ? 1 + 3 * NP : 1 + NP;
+    const int slotStride = NF * rowStride;
+    float* const scr = reinterpret_cast<float*>(p.scratch);
+    float* fs = scr;  // the slot of the current unit round
     const int myCol = int(blockIdx.x) * RB + tid;
+    const int seedRow = nSteps * Ti;
 
     // Gaussian of a lower-half integer draw up in [1, 2^31] (uniform up / denom of the
     // generator; sup: the draw was in the upper half): the piece is the leading bit of up and
@@ -216,8 +222,8 @@ __global__ void __launch_bounds__(RB, 8) dupire_risk32(const McParams p)
                     if (last) bLast[a] = alive[a];
                     else
                     {
-                        scr[(F_B + a) * rowStride + i * Ti + myCol] = alive[a];
-                        scr[(F_S + a) * rowStride + i * Ti + myCol] = S;
+                        fs[(F_B + a) * rowStride + i * Ti + myCol] = alive[a];
+                        fs[(F_S + a) * rowStride + i * Ti + myCol] = S;
                     }
                     alive[a] *= (barSmooth - S) / twoSmooth;
                     flag[a] = 1;
@@ -238,7 +244,7 @@ __global__ void __launch_bounds__(RB, 8) dupire_risk32(const McParams p)
         for (int s = 0; s < nSteps; ++s)
         {
             const float g = gen(s);
-            __stcs(scr + F_G * rowStride + s * Ti + myCol, g);  // streamed: read once, in the reverse
+            __stcs(fs + F_G * rowStride + s * Ti + myCol, g);  // streamed: read once, in the reverse
             const float2* trow = td + size_t(s) * tPitch;
 #pragma unroll
             for (int a = 0; a < NP; ++a)
@@ -251,7 +257,7 @@ __global__ void __launch_bounds__(RB, 8) dupire_risk32(const McParams p)
                 const unsigned tq = __float_as_uint(t2) & T_MASK;
                 const float2 yd = __ldg(trow + lo);
                 const float v = fmaf(yd.y, t2 - 2.0f, yd.x);
-                __stcs(reinterpret_cast<unsigned*>(scr) + (F_W + a) * rowStride + s * Ti + myCol,
+                __stcs(reinterpret_cast<unsigned*>(fs) + (F_W + a) * rowStride + s * Ti + myCol,
                        (unsigned(lo) << LO_SHIFT) | (flag[a] ? BAND_BIT : 0u) | tq);
                 flag[a] = 0;  // the flag of point s + 1 is set by its date, if any
                 x[a] += v * (-0.5f * v + ga);
@@ -299,6 +305,11 @@ __global__ void __launch_bounds__(RB, 8) dupire_risk32(const McParams p)
             axOut[a] = ax;
             alOut[a] = aAl;
             live[a] = ax != 0.0f || aAl != 0.0f;
+            if (live[a])
+            {
+                fs[(F_W + a) * rowStride + seedRow + myCol] = ax;
+                if (UOC) fs[(F_B + a) * rowStride + seedRow + myCol] = aAl;
+            }
         }
     };
 
@@ -311,14 +322,19 @@ __global__ void __launch_bounds__(RB, 8) dupire_risk32(const McParams p)
     };
 
     // ---------------------------------------------------------------------------------
-    // Compaction and reverse sweep of one unit round, then the round's slab -> gnode.
+    // Pending-path list: a first-in-first-out ring of LIST_CAP entries in shared memory.
+    // head, q2 and q1 are uniform over the block: q2 entries of round r-2 and then q1 of round
+    // r-1 are pending at the start of round r (q2 + q1 < RB).
     // ---------------------------------------------------------------------------------
-    auto reverse = [&]() {
+    int head = 0, q2 = 0, q1 = 0;
+
+    // Appends the round's live paths (slot `slot`) behind the pending ones; returns how many.
+    auto collect = [&](int slot) -> int {
         const unsigned b0 = __ballot_sync(0xffffffffu, live[0]);
         const unsigned b1 = NP == 2 ? __ballot_sync(0xffffffffu, live[NP - 1]) : 0u;
         if (lane == 0) cnt[wib] = __popc(b0) + __popc(b1);
         __syncthreads();
-        int total = 0, off = 0;
+        int total = 0, off = head + q2 + q1;
 #pragma unroll
         for (int w = 0; w < RW; ++w)
         {
@@ -328,62 +344,77 @@ __global__ void __launch_bounds__(RB, 8) dupire_risk32(const McParams p)
         }
         const unsigned lt = (1u << lane) - 1u;
         if (live[0])
-        {
-            const int pos = off + __popc(b0 & lt);
-            listIdx[pos] = tid * 2;
-            listAx[pos] = axOut[0];
-            listAl[pos] = alOut[0];
-        }
+            listIdx[(off + __popc(b0 & lt)) & (LIST_CAP - 1)] = (unsigned short)((slot << 8) | (tid << 1));
         if (NP == 2 && live[NP - 1])
-        {
-            const int pos = off + __popc(b0) + __popc(b1 & lt);
-            listIdx[pos] = tid * 2 + 1;
-            listAx[pos] = axOut[NP - 1];
-            listAl[pos] = alOut[NP - 1];
-        }
+            listIdx[(off + __popc(b0) + __popc(b1 & lt)) & (LIST_CAP - 1)] =
+                (unsigned short)((slot << 8) | (tid << 1) | 1);
         __syncthreads();
-        for (int idx = tid; idx < total; idx += RB)
+        return total;
+    };
+
+    // Sweeps the first n (uniform, 1..RB) pending paths back, one per thread, then moves the
+    // chunk's slab into this thread's words of the block's int64 slab.
+    auto sweep = [&](int n) {
+        if (tid < n)
         {
-            const int e = listIdx[idx];
+            const int e = listIdx[(head + tid) & (LIST_CAP - 1)];
             const int a = e & 1;
-            const int col = int(blockIdx.x) * RB + (e >> 1);
-            float ax = listAx[idx], aAl = listAl[idx];
-            const unsigned* sw = reinterpret_cast<const unsigned*>(scr) + (F_W + a) * rowStride + col;
-            const float* sg = scr + F_G * rowStride + col;
+            const int col = int(blockIdx.x) * RB + ((e >> 1) & (RB - 1));
+            const float* es = scr + (e >> 8) * slotStride;  // the path's ring slot
+            float ax = es[(F_W + a) * rowStride + seedRow + col];
+            float aAl = UOC ? es[(F_B + a) * rowStride + seedRow + col] : 0.0f;
+            const unsigned* sw = reinterpret_cast<const unsigned*>(es) + (F_W + a) * rowStride + col;
+            const float* sg = es + F_G * rowStride + col;
             unsigned wNext = 0;  // packed word of the step after s: band flag of point s + 1
-            // the step words and Gaussians are loaded two steps ahead
-            unsigned wq0 = __ldcs(sw + (nSteps - 1) * Ti), wq1 = 0;
-            float gq0 = __ldcs(sg + (nSteps - 1) * Ti), gq1 = 0.0f;
+            // software pipeline: the step words and Gaussians are loaded three steps ahead
+            // (they come from DRAM), the local-vol entry and interval record of a step one
+            // step ahead, so that only the adjoint itself is carried from step to step
+            unsigned wA = __ldcs(sw + (nSteps - 1) * Ti), wB = 0, wC = 0;
+            float gA = __ldcs(sg + (nSteps - 1) * Ti), gB = 0.0f, gC = 0.0f;
             if (nSteps >= 2)
             {
-                wq1 = __ldcs(sw + (nSteps - 2) * Ti);
-                gq1 = __ldcs(sg + (nSteps - 2) * Ti);
+                wB = __ldcs(sw + (nSteps - 2) * Ti);
+                gB = __ldcs(sg + (nSteps - 2) * Ti);
             }
+            if (nSteps >= 3)
+            {
+                wC = __ldcs(sw + (nSteps - 3) * Ti);
+                gC = __ldcs(sg + (nSteps - 3) * Ti);
+            }
+            float2 ydA = __ldg(td + size_t(nSteps - 1) * tPitch + int(wA >> LO_SHIFT));
+            float2 irA = sIr[wA >> LO_SHIFT];
             for (int s = nSteps - 1; s >= 0; --s)
             {
                 if (UOC && (wNext & BAND_BIT))
                 {
                     const int i = s + 1;
-                    const float before = scr[(F_B + a) * rowStride + i * Ti + col];
-                    const float S = scr[(F_S + a) * rowStride + i * Ti + col];
+                    const float before = es[(F_B + a) * rowStride + i * Ti + col];
+                    const float S = es[(F_S + a) * rowStride + i * Ti + col];
                     const float aF = aAl * before * invTwo;
                     aAl *= (barSmooth - S) / twoSmooth;
                     ax += aF * S;
                 }
-                const unsigned W = wq0;
-                const float g1 = gq0;
-                wq0 = wq1;
-                gq0 = gq1;
-                if (s >= 2)
+                const unsigned W = wA;
+                const float g1 = gA;
+                const float2 yd = ydA, ir = irA;
+                wA = wB;
+                gA = gB;
+                wB = wC;
+                gB = gC;
+                if (s >= 3)
                 {
-                    wq1 = __ldcs(sw + (s - 2) * Ti);
-                    gq1 = __ldcs(sg + (s - 2) * Ti);
+                    wC = __ldcs(sw + (s - 3) * Ti);
+                    gC = __ldcs(sg + (s - 3) * Ti);
+                }
+                if (s >= 1)
+                {
+                    const int loN = int(wA >> LO_SHIFT);
+                    ydA = __ldg(td + size_t(s - 1) * tPitch + loN);
+                    irA = sIr[loN];
                 }
                 const float ga = a ? -g1 : g1;
                 const int lo = int(W >> LO_SHIFT);
                 const float t = __uint_as_float(TWO_BITS | (W & T_MASK)) - 2.0f;
-                const float2 yd = __ldg(td + size_t(s) * tPitch + lo);
-                const float2 ir = sIr[lo];
                 const float v = fmaf(yd.y, t, yd.x);
                 const float av = ax * (ga - v);      // d x_{s+1} / d v = g - v
                 ax += av * (yd.y * ir.y);            // d x_{s+1} / d x_s = 1 + (g - v) dv/dx
@@ -415,14 +446,15 @@ __global__ void __launch_bounds__(RB, 8) dupire_risk32(const McParams p)
             }
             if (UOC && (wNext & BAND_BIT))  // band at today's date
             {
-                const float before = scr[(F_B + a) * rowStride + col];
-                const float S = scr[(F_S + a) * rowStride + col];
+                const float before = es[(F_B + a) * rowStride + col];
+                const float S = es[(F_S + a) * rowStride + col];
                 ax += aAl * before * invTwo * S;
             }
             fix_add(&slab[0], ax / spot);  // x_0 = log(spot)
         }
+        head += n;
         __syncthreads();
-        // the round's slab -> this thread's words of the block's int64 slab
+        // the chunk's slab -> this thread's words of the block's int64 slab
         for (int i = tid; i < nNodes; i += RB)
         {
             const int v = node[i];
@@ -432,6 +464,32 @@ __global__ void __launch_bounds__(RB, 8) dupire_risk32(const McParams p)
                 gnode[i] += v;
             }
         }
+        __syncthreads();  // the next chunk adds into the cleared slab
+    };
+
+    // End of round r (its paths in ring slot `slot`; slot < 0: after the last round): list its
+    // live paths, sweep full chunks, and sweep the rest if paths of round r-2 are still pending
+    // (round r+1 rewrites their slot) or no round follows.  The trip counts depend only on
+    // uniform values, so every barrier is reached by the whole block.
+    auto endRound = [&](int slot) {
+        const int count = q2 + q1 + (slot >= 0 ? collect(slot) : 0);
+        int done = 0;
+        for (;;)
+        {
+            const int left = count - done;
+            const int n = left >= RB ? RB : (done < q2 || slot < 0) ? left : 0;
+            if (n == 0) break;
+            sweep(n);
+            done += n;
+        }
+        const int old = q2 + q1 - done;  // round r-1's paths still pending
+        q2 = old > 0 ? old : 0;
+        q1 = count - done - q2;
+    };
+    auto slotOf = [&](long long it) {
+        const int k = int(it % R32_RING);
+        fs = scr + k * slotStride;
+        return k;
     };
 
     const long long T = (long long)gridDim.x * RB;
@@ -448,12 +506,13 @@ __global__ void __launch_bounds__(RB, 8) dupire_risk32(const McParams p)
         {
             const long long u = u0 + it;
             const int nAct = u < u1 ? ((2 * u + 1 < p.nPath) ? 2 : 1) : 0;
+            const int slot = slotOf(it);
             forward(nAct, [&](int) {
                 const unsigned d = mrg_next(st);   // in [1, m1]; uniform d / (m1 + 1)
                 const bool sup = d > 2147483544u;  // (m1 + 1) / 2
                 return gaussT(sup ? 4294967088u - d : d, sup);
             });
-            reverse();
+            endRound(slot);
         }
     }
     else
@@ -478,14 +537,16 @@ __global__ void __launch_bounds__(RB, 8) dupire_risk32(const McParams p)
                 const long long n = b * 32 + lane;
                 nAct = (n >= 1 && n <= p.nPath) ? 1 : 0;
             }
+            const int slot = slotOf(it);
             forward(nAct, [&](int i) {
                 const unsigned sb = base[i] ^ sobol_state(p.sobolDir, nSteps, i, (unsigned long long)lane);
                 const bool sup = sb >= 2147483648u;
                 return gaussT(sup ? 0u - sb : (sb > 1u ? sb : 1u), sup);  // state 0 occurs only at index 0
             });
-            reverse();
+            endRound(slot);
         }
     }
+    endRound(-1);  // the paths still pending after the last round
 
     __syncthreads();
     if (tid == 0) fix_flush(&p.acc[0], &slab[0]);

@@ -30,19 +30,32 @@ int mc_smem_bytes(const McLaunch& l, const McParams& p, int stageY, size_t* byte
     return 0;
 }
 
-int mc_scratch_fields(const McLaunch& l)
+long long mc_rounds(const McLaunch& l, long long nPath, long long threads)
+{
+    if (threads < 32) threads = 32;
+    if (l.rng == RNG_SOBOL)  // warp batches of 32 indices
+    {
+        const long long batches = nPath / 32 + 1, warps = threads / 32;
+        return (batches + warps - 1) / warps;
+    }
+    const long long units = (nPath + 1) / 2;  // antithetic pairs
+    return (units + threads - 1) / threads;
+}
+
+int mc_scratch_fields(const McLaunch& l, long long rounds)
 {
     const int NP = l.rng == RNG_SOBOL ? 1 : 2;
-    // dupire_risk32: Gaussian, packed step word per path, and for the barrier the survival
-    // factor and spot of band dates per path; generic kernel: Gaussian, state per path, and
-    // for the barrier the survival factor of band dates per path
-    if (l.fast) return 1 + NP + (l.prod == PROD_UOC ? 2 * NP : 0);
+    // dupire_risk32, per ring slot: Gaussian, packed step word per path, and for the barrier
+    // the survival factor and spot of band dates per path; generic kernel: Gaussian, state per
+    // path, and for the barrier the survival factor of band dates per path
+    const int slots = int(rounds < 1 ? 1 : rounds < R32_RING ? rounds : R32_RING);
+    if (l.fast) return slots * (1 + NP + (l.prod == PROD_UOC ? 2 * NP : 0));
     return 1 + NP + (l.prod == PROD_UOC ? NP : 0);
 }
 
 size_t mc_scratch_bytes(const McLaunch& l, McParams& p, long long grid)
 {
-    const size_t fields = size_t(mc_scratch_fields(l)) * size_t(p.nSteps + 1) * size_t(grid) * 128 * (l.fp32 ? 4 : 8);
+    const size_t fields = size_t(p.scratchFields) * size_t(p.nSteps + 1) * size_t(grid) * 128 * (l.fp32 ? 4 : 8);
     if (!l.fast)
     {
         p.nodeSlabOffset = 0;

@@ -155,16 +155,17 @@ extern "C" int cf_aad_risk_aggregate_noalloc(cf_context* ctx, const char* modelI
         mc_smem_bytes(l, p, 0, &smem);
         if ((rc = mc_occupancy(l, smem, &occ)) || occ < 1) return fail_c(CF_E_SHAPE, "noalloc: kernel does not fit");
     }
-    p.scratchFields = mc_scratch_fields(l);
-    // scratch per block: the reverse-sweep fields of 128 threads, plus the FP32 kernel's
-    // int64 node slab (and 256 bytes of alignment between the two regions)
-    const size_t perThread = size_t(p.scratchFields) * size_t(plan->nSteps + 1) * (fp32 ? 4 : 8);
+    // scratch per block: the reverse-sweep fields of 128 threads (counted for the FP32 kernel's
+    // full ring of round slots), plus its int64 node slab (and 256 bytes of alignment between
+    // the two regions)
+    const size_t perThread = size_t(mc_scratch_fields(l, R32_RING)) * size_t(plan->nSteps + 1) * (fp32 ? 4 : 8);
     const size_t perBlock = perThread * 128 + (l.fast ? size_t(p.nS) * size_t(p.nT) * 8 : 0);
     const long long fitBlocks = (long long)((CF_NOALLOC_BYTES - offScr - 256) / perBlock);
     if (fitBlocks < 1) return fail_c(CF_E_SHAPE, "noalloc: one block of reverse-sweep scratch exceeds the arena");
     const long long threadsNeeded = sobol ? (p.nPath / 32 + 1) * 32 : (p.nPath + 1) / 2;
     long long grid = std::min<long long>((threadsNeeded + 127) / 128, (long long)c.numSMs * occ);
     grid = std::max(1LL, std::min(grid, fitBlocks));
+    p.scratchFields = mc_scratch_fields(l, mc_rounds(l, p.nPath, grid * 128));
     if (mc_scratch_bytes(l, p, grid) > CF_NOALLOC_BYTES - offScr)
         return fail_c(CF_E_SHAPE, "noalloc: reverse-sweep scratch exceeds the arena");
     l.grid = int(grid);

@@ -49,11 +49,11 @@ def test_results_identical_alone_and_in_the_mix(eng):
 
 
 def test_admission_budget_rejection_and_failures(eng):
-    # A 60x30 barrier risk request at 2^16 FP32 paths holds ~103 MB of reverse-sweep scratch
-    # (5 fields x 157 dates x 2^15 threads x 4 B); the same at 2^22 paths holds the scratch of
-    # the full resident grid (~0.4 GB).  A 250 MB budget runs two small ones at a time and
-    # rejects the large one.
-    srv = Server(eng, slots=4, hbm_budget=250 << 20)
+    # A 60x30 barrier risk request at 2^16 FP32 paths runs one unit round and holds ~148 MB of
+    # reverse-sweep scratch (7 fields x 157 dates x 2^15 threads x 4 B, plus the blocks' node
+    # slabs); the same at 2^22 paths holds three round slots for the full resident grid
+    # (~2 GB).  A 320 MB budget runs two small ones at a time and rejects the large one.
+    srv = Server(eng, slots=4, hbm_budget=320 << 20)
     r = dict(kind="risk", model="dup100_60x30w", product="uoc100_1_1.4_156", paths=1 << 16, sobol=False)
     big = dict(r, paths=1 << 22)
     ids = [srv.submit("risk", r["model"], r["product"], num_of(r)) for _ in range(6)]
@@ -61,7 +61,7 @@ def test_admission_budget_rejection_and_failures(eng):
     assert srv.wait(rej) == "rejected" and "budget" in srv.error()
     assert all(srv.wait(i) == "done" for i in ids)
     st = srv.stats()
-    assert st["maxInFlight"] <= 2 and st["peakFootprint"] <= 250 << 20
+    assert st["maxInFlight"] <= 2 and st["peakFootprint"] <= 320 << 20
     # the next two starts fail (an allocation failure injected on the host)
     srv.inject_failures(2)
     bad = [srv.submit("value", "bs100", "eu100_1", num_of(dict(paths=1 << 14, sobol=True))) for _ in range(2)]

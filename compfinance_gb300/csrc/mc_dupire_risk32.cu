@@ -44,8 +44,10 @@ constexpr int LO_SHIFT = T_BITS + 1;    // interval index in bits 23..31
 // are round(t 2^22): no conversion instruction either way
 constexpr unsigned TWO_BITS = 0x40000000u;         // bits of 2.0f
 constexpr float T_MAX = 1.0f - 1.0f / 4194304.0f;  // t + 2 stays below 3
-// Contributions with |adjoint| >= AV_MAX go exactly to the global accumulators instead of
-// the int32 slab (the host's choice of nodeShiftF assumes this bound).
+// Contributions with |adjoint| >= AV_MAX go to the block's int64 node slab in global memory
+// (native 64-bit adds, same unit) instead of the int32 shared slab (the host's choice of
+// nodeShiftF assumes this bound).  After a path passes through the barrier's smoothing band
+// its state adjoint is of the order of the spot over the band width, so this is common.
 constexpr float AV_MAX = 512.0f;
 // pending-path list: a power of two above the most it holds (127 left over + 2 RB new)
 constexpr int LIST_CAP = 512;
@@ -105,8 +107,9 @@ __global__ void __launch_bounds__(RB, 8) dupire_risk32(const McParams p)
 
     const int tid = threadIdx.x, lane = tid & 31, wib = tid >> 5;
     const int nS = p.nS, nT = p.nT, nSteps = p.nSteps, nPay = p.nPay, nNodes = nS * nT;
-    // block-private int64 node slab in global memory, after the scratch fields; word i is
-    // read and written only by thread i mod RB
+    // block-private int64 node slab in global memory, after the scratch fields: during a sweep
+    // it takes the large contributions (64-bit atomic adds); between sweeps word i is read and
+    // written only by thread i mod RB
     long long* gnode = reinterpret_cast<long long*>(static_cast<char*>(p.scratch) + p.nodeSlabOffset) +
                        size_t(blockIdx.x) * nNodes;
     const float wScale = ldexpf(1.0f, p.nodeShiftF);
@@ -313,12 +316,17 @@ __global__ void __launch_bounds__(RB, 8) dupire_risk32(const McParams p)
         }
     };
 
-    // contribution c (units of 1) to spot j of step s's vol row: exact global fixed point when
-    // too large for the slab
-    auto bigAdd = [&](int s, int j, float c) {
-        fix_add(&p.acc[2 * (1 + j * nT + __ldg(p.colA + s))], c * __ldg(p.cAf + s));
-        const float cb = __ldg(p.cBf + s);
-        if (cb != 0.0f) fix_add(&p.acc[2 * (1 + j * nT + __ldg(p.colB + s))], c * cb);
+    // contribution c (units of 1) to spot j of a step's vol row (its columns and weights in
+    // sc), too large for the shared slab: into the block's int64 slab, rounded once like the
+    // shared adds.  gnode is written only by these adds during a sweep and only by its owning
+    // thread between sweeps (barriers in between).
+    auto bigAdd = [&](const int4 sc, int j, float c) {
+        long long* g = gnode + j * nT;
+        atomicAdd(reinterpret_cast<unsigned long long*>(g + sc.x),
+                  (unsigned long long)__float2ll_rn(c * __int_as_float(sc.z)));
+        const float wb = __int_as_float(sc.w);
+        if (wb != 0.0f)
+            atomicAdd(reinterpret_cast<unsigned long long*>(g + sc.y), (unsigned long long)__float2ll_rn(c * wb));
     };
 
     // ---------------------------------------------------------------------------------
@@ -423,9 +431,9 @@ __global__ void __launch_bounds__(RB, 8) dupire_risk32(const McParams p)
                     const int jl = lo - (lo > 0 ? 1 : 0);
                     const bool inner = lo > 0 && lo < nS;  // two spot knots; one at the flat ends
                     const float cR = av * t, cL = av - cR;
+                    const int4 sc = stepc[s];
                     if (fabsf(av) < AV_MAX)
                     {
-                        const int4 sc = stepc[s];
                         const float wa = __int_as_float(sc.z), wb = __int_as_float(sc.w);
                         int* nl = node + jl * nT;
                         atomicAdd(nl + sc.x, __float2int_rn(cL * wa));
@@ -438,8 +446,8 @@ __global__ void __launch_bounds__(RB, 8) dupire_risk32(const McParams p)
                     }
                     else
                     {
-                        bigAdd(s, jl, cL);
-                        if (inner && cR != 0.0f) bigAdd(s, jl + 1, cR);
+                        bigAdd(sc, jl, cL);
+                        if (inner && cR != 0.0f) bigAdd(sc, jl + 1, cR);
                     }
                 }
                 wNext = W;
@@ -461,7 +469,7 @@ __global__ void __launch_bounds__(RB, 8) dupire_risk32(const McParams p)
             if (v)
             {
                 node[i] = 0;
-                gnode[i] += v;
+                gnode[i] = __ldcg(gnode + i) + v;  // L2: the sweep's 64-bit adds land there
             }
         }
         __syncthreads();  // the next chunk adds into the cleared slab
@@ -553,7 +561,7 @@ __global__ void __launch_bounds__(RB, 8) dupire_risk32(const McParams p)
     // node words in units of 2^-nodeShiftF (nodeShiftF <= FIX_HI_SHIFT): exact in the hi word
     for (int i = tid; i < nNodes; i += RB)
     {
-        const long long v = gnode[i];
+        const long long v = __ldcg(gnode + i);
         if (v) atomicAdd(reinterpret_cast<unsigned long long*>(&p.acc[2 * (1 + i)]),
                          (unsigned long long)(v << (FIX_HI_SHIFT - p.nodeShiftF)));
     }

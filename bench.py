@@ -35,7 +35,7 @@ METRIC = "AAD-risk paths/s (Dupire barrier), FP32 vs FP64 at equal error; serve 
 NPATH = 1 << 22
 GRID = (60, 30)
 FLOPS_PER_PATH_STEP = 53.0   # algorithmic FP work of value + adjoint per path-step (mrg32k3a)
-TRAFFIC_BYTES_PER_PATH_STEP = 10.56  # measured DRAM traffic of the FP32 risk launch per path-step
+TRAFFIC_BYTES_PER_PATH_STEP = 11.35  # measured DRAM traffic of the FP32 risk launch per path-step
 CONFIG = {
     "workload": "dupire_uoc_aad_risk_60x30_156steps_2^22paths_fp32path",
     "model": "Dupire local vol 60x30 (50-200 log-spaced x 0.1-3.0y), seeded synthetic surface",
@@ -43,8 +43,8 @@ CONFIG = {
     "rng": "mrg32k3a(12345,1234) antithetic",
     "paths": NPATH,
     "risks": 1801,
-    "l2": "flushed between steps (256 MiB write outside the per-step events); per-thread reverse-sweep "
-          "scratch of ~0.4 GB also exceeds L2",
+    "l2": "flushed between steps (256 MiB write outside the per-step events); the reverse-sweep scratch "
+          "(three unit-round slots, ~2 GB) also exceeds L2",
 }
 
 
@@ -179,16 +179,21 @@ def serving_leg(eng, n, seed):
     portfolio AADriskMulti), FP32 path form, 64 GB admission budget, 8 slots; then the same
     requests all submitted at once (the server's batch throughput) and one at a time through the
     synchronous entry points."""
+    from compfinance_gb300.api import Server
     from compfinance_gb300.serve_stream import load_store, run_one_at_a_time, run_stream
     models, products = W.serving_store()
     load_store(eng, models, products)
     stream = W.serving_stream(n=n, rate=2000.0, seed=seed)
     for r in stream:  # lower every plan and warm each kernel variant before timing
         eng.shapes(r["model"], r["product"])
-    run_stream(eng, W.serving_stream(n=64, rate=1e6, seed=seed + 1), slots=8)
-    stats, makespan, status, _ = run_stream(eng, stream, slots=8, budget=64 << 30)
-    # batch: the same requests all submitted at once to the same server (its capacity)
-    bstats, bmakespan, _, _ = run_stream(eng, [dict(r, t=0.0) for r in stream], slots=8, budget=64 << 30)
+    # one server for every stream below: 8 slots, 64 GB admission budget.  The batch (the same
+    # requests all submitted at once: the server's capacity) runs once untimed first, which
+    # also grows every slot's device buffers to the stream's sizes, as a long-running server's are.
+    srv = Server(eng, slots=8, hbm_budget=64 << 30)
+    batch_reqs = [dict(r, t=0.0) for r in stream]
+    run_stream(eng, batch_reqs, server=srv)
+    stats, makespan, status, _ = run_stream(eng, stream, server=srv)
+    bstats, bmakespan, _, _ = run_stream(eng, batch_reqs, server=srv)
     t_seq, steps = run_one_at_a_time(eng, stream)
     served = stats["pathStepsDone"] / makespan
     batch_all = bstats["pathStepsDone"] / bmakespan
@@ -199,13 +204,13 @@ def serving_leg(eng, n, seed):
     for frac in (0.8, 0.9):
         rate = frac * n / bmakespan
         scaled = [dict(r, t=r["t"] * 2000.0 / rate) for r in stream]
-        lstats, lmakespan, _, _ = run_stream(eng, scaled, slots=8, budget=64 << 30)
+        lstats, lmakespan, _, _ = run_stream(eng, scaled, server=srv)
         load.append({"offered_over_batch": frac, "arrival_rate_req_s": rate,
                      "completed": lstats["completed"], "failed": lstats["failed"],
                      "p50_ms": lstats["p50Ms"], "p99_ms": lstats["p99Ms"], "mean_ms": lstats["meanMs"],
                      "makespan_s": lmakespan,
                      "served_over_batch": lstats["pathStepsDone"] / lmakespan / batch_all})
-    return {"requests": n, "arrival_rate_req_s": 2000.0, "slots": 8, "hbm_budget_gb": 64,
+    out = {"requests": n, "arrival_rate_req_s": 2000.0, "slots": 8, "hbm_budget_gb": 64,
             "completed": stats["completed"], "failed": stats["failed"], "rejected": stats["rejected"],
             "p50_ms": stats["p50Ms"], "p99_ms": stats["p99Ms"], "mean_ms": stats["meanMs"],
             "makespan_s": makespan, "served_path_steps_per_s": served,
@@ -213,6 +218,8 @@ def serving_leg(eng, n, seed):
             "one_at_a_time_s": t_seq, "one_at_a_time_path_steps_per_s": batch,
             "served_over_one_at_a_time": served / batch, "max_in_flight": stats["maxInFlight"],
             "peak_footprint_gb": stats["peakFootprint"] / 2**30, "load_sweep": load}
+    srv.close()
+    return out
 
 
 def grid_sweep(eng, stream, flush, npath):

@@ -546,5 +546,9 @@ class Server:
         _check(lib().cf_server_stats(self._h, ctypes.byref(s)))
         return {k: getattr(s, k) for k, _ in CfServingStats._fields_}
 
+    def reset_stats(self):
+        """Starts the statistics afresh; the slots keep their streams and device buffers."""
+        _check(lib().cf_server_reset_stats(self._h))
+
     def inject_failures(self, n):
         _check(lib().cf_server_inject_failures(self._h, int(n)))

@@ -289,6 +289,14 @@ int cf_server_stats(cf_server* s, cf_serving_stats* out)
     return CF_OK;
 }
 
+int cf_server_reset_stats(cf_server* s)
+{
+    if (!s) return fail(CF_E_ARG, "null server");
+    std::lock_guard<std::mutex> l(s->mu);
+    s->sched.resetStats();
+    return CF_OK;
+}
+
 int cf_server_inject_failures(cf_server* s, int startFailures)
 {
     if (!s) return fail(CF_E_ARG, "null server");

@@ -185,6 +185,18 @@ public:
         return i + 1 < v.size() ? v[i] * (1 - f) + v[i + 1] * f : v[i];
     }
 
+    // Clears the counters and latencies (not the queue, nor the memory in use); peak restarts
+    // from what is in use now.
+    void resetStats()
+    {
+        submitted_ = completed_ = failed_ = rejected_ = cancelled_ = timedOut_ = 0;
+        peak_ = inUse_;
+        maxInFlight_ = 0;
+        busy_ = 0;
+        workDone_ = 0;
+        latencies_.clear();
+    }
+
     uint64_t submitted_ = 0, completed_ = 0, failed_ = 0, rejected_ = 0, cancelled_ = 0, timedOut_ = 0;
     size_t inUse_ = 0, peak_ = 0;
     int maxInFlight_ = 0;

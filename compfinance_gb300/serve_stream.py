@@ -45,9 +45,13 @@ def run_one_at_a_time(eng, stream, precision="fp32"):
     return time.perf_counter() - t0, steps
 
 
-def run_stream(eng, stream, slots=8, budget=64 << 30, precision="fp32", keep_results=False):
-    """Submit each request at its arrival time; returns stats, makespan and (optionally) results."""
-    srv = Server(eng, slots=slots, hbm_budget=budget)
+def run_stream(eng, stream, slots=8, budget=64 << 30, precision="fp32", keep_results=False, server=None):
+    """Submit each request at its arrival time; returns stats, makespan and (optionally) results.
+    With `server`, the stream runs on that server (its statistics reset first, its slots and
+    their device buffers kept); otherwise on a new server of `slots` slots and `budget` bytes."""
+    srv = server or Server(eng, slots=slots, hbm_budget=budget)
+    if server is not None:
+        srv.reset_stats()
     ids = [None] * len(stream)
     t0 = time.perf_counter()
 
@@ -70,5 +74,6 @@ def run_stream(eng, stream, slots=8, budget=64 << 30, precision="fp32", keep_res
             results[i] = srv.result(rid)
     makespan = time.perf_counter() - t0
     stats = srv.stats()
-    srv.close()
+    if server is None:
+        srv.close()
     return stats, makespan, status, results

@@ -297,6 +297,9 @@ int cf_server_result(cf_server* server, uint64_t id, double* values, double* std
 /* Forgets a finished request (frees its result storage). */
 int cf_server_release(cf_server* server, uint64_t id);
 int cf_server_stats(cf_server* server, cf_serving_stats* stats);
+/* Starts the statistics afresh (counters, latencies, peaks) on a server that keeps its slots
+   and their device buffers, e.g. between a warm-up stream and a measured one. */
+int cf_server_reset_stats(cf_server* server);
 /* Test hook: the next n request starts fail as if a device allocation had failed. */
 int cf_server_inject_failures(cf_server* server, int startFailures);
 

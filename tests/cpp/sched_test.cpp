@@ -74,6 +74,20 @@ int main()
         check(ex.startOrder == ids, "arrival_order");
         check(s.peak_ <= 100 && s.maxInFlight_ == 2, "peak_footprint");
     }
+    {  // statistics reset between streams: counters restart, the memory in use stays accounted
+        FakeExec ex;
+        Scheduler<FakeExec> s(ex, 2, 100);
+        for (int i = 0; i < 3; ++i) s.submit(40, 0, 0);
+        s.step(0);
+        ex.now = 1;
+        s.step(1);  // two finish, the third starts
+        s.resetStats();
+        check(s.completed_ == 0 && s.latencies_.empty() && s.workDone_ == 0, "reset_clears_counters");
+        check(s.peak_ == s.inUse_ && s.inUse_ == 40, "reset_keeps_in_use", std::to_string(s.inUse_));
+        ex.now = 2;
+        s.step(2);
+        check(s.completed_ == 1 && s.latencies_.size() == 1 && s.inUse_ == 0, "reset_then_complete");
+    }
     {  // slot-limited admission; small requests overlap
         FakeExec ex;
         Scheduler<FakeExec> s(ex, 3, 1000);

@@ -615,6 +615,8 @@ int Context::buildPlan(const ModelDesc& m, const ProductDesc& pd, Plan& plan)
     if (rc) return rc;
     CF_CUDA(cudaMemcpyAsync(plan.tables.ptr, pk.buf.data(), pk.buf.size(), cudaMemcpyHostToDevice, stream));
     h2d += pk.buf.size();
+    // the tables are read by kernels on any slot's stream: the upload completes here
+    CF_CUDA(cudaStreamSynchronize(stream));
     unsigned char* d = static_cast<unsigned char*>(plan.tables.ptr);
     auto D = [&](size_t off) { return static_cast<const void*>(d + off); };
     if (m.kind == MODEL_BS)
@@ -710,6 +712,13 @@ int Context::getPlan(const std::string& mid, const std::string& pid, Plan*& out)
         return CF_OK;
     }
     auto plan = std::make_unique<Plan>();
+    if (it != plans.end())
+    {
+        // the model or product changed: the new plan takes over the stale plan's device tables
+        // once no kernel can still read them (a device-wide wait, as freeing them would be)
+        CF_CUDA(cudaDeviceSynchronize());
+        plan->tables.swap(it->second->tables);
+    }
     int rc = buildPlan(mi->second, pi->second, *plan);
     if (rc) return rc;
     plan->mver = mi->second.version;

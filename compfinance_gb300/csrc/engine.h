@@ -6,6 +6,7 @@
 #include <memory>
 #include <mutex>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/cfgpu.h"
@@ -36,6 +37,11 @@ struct DevBuf
     DevBuf(const DevBuf&) = delete;
     DevBuf& operator=(const DevBuf&) = delete;
     ~DevBuf() { release(); }
+    void swap(DevBuf& o)
+    {
+        std::swap(ptr, o.ptr);
+        std::swap(bytes, o.bytes);
+    }
 };
 
 // A model of the store (store.h:38-94): Black-Scholes, Dupire, or multiple correlated

@@ -129,6 +129,7 @@ struct McParams
 
     // events
     const int* evAtStep;  // [nSteps+1] product date index reached at timeline point i, or -1
+    int evEvery;          // 1 when every point after today is a product date
     const int* evPoint;   // [nEv] timeline point of product date e
     const double* evD;    // [10][nEv]: ff, tauF, disc, tauD, numeraire (factor), t, needNum,
                           // libor(t_e, t_e+1), its derivative to the rate, coverage t_e+1 - t_e

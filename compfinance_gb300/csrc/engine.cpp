@@ -658,6 +658,9 @@ int Context::buildPlan(const ModelDesc& m, const ProductDesc& pd, Plan& plan)
     P.evPayOff = (const int*)D(oPo);
     P.sobolDir = plan.sobolOk ? (const unsigned*)D(oDir) : nullptr;
     plan.evAtStep = evAtStep;
+    P.evEvery = 1;
+    for (int i = 1; i <= plan.nSteps; ++i)
+        if (evAtStep[i] < 0) P.evEvery = 0;
     return CF_OK;
 }
 

@@ -154,6 +154,7 @@ __global__ void __launch_bounds__(RB, 8) dupire_risk32(const McParams p)
     float* fs = scr;  // the slot of the current unit round
     const int myCol = int(blockIdx.x) * RB + tid;
     const int seedRow = nSteps * Ti;
+    const bool evEvery = p.evEvery != 0;
 
     // Gaussian of a lower-half integer draw up in [1, 2^31] (uniform up / denom of the
     // generator; sup: the draw was in the upper half): the piece is the leading bit of up and
@@ -265,7 +266,8 @@ __global__ void __launch_bounds__(RB, 8) dupire_risk32(const McParams p)
                 flag[a] = 0;  // the flag of point s + 1 is set by its date, if any
                 x[a] += v * (-0.5f * v + ga);
             }
-            if (__ldg(p.evAtStep + s + 1) >= 0)
+            // the barrier monitors at dates only; a European's one date is the last point
+            if (UOC ? (evEvery || __ldg(p.evAtStep + s + 1) >= 0) : s + 1 == nSteps)
 #pragma unroll
                 for (int a = 0; a < NP; ++a)
                     if (a < nAct) event(s + 1, a);

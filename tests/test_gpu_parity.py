@@ -230,3 +230,27 @@ def test_fp32_risk_kernel_small_and_odd_path_counts(mc_eng):
             scale = max(np.abs(r64["risks"]).max(), 1e-3)
             assert np.abs(r32["risks"] - r64["risks"]).max() <= 5e-3 * scale, (n, sob)
             assert abs(r32["payoffValues"][0] - r64["payoffValues"][0]) <= 1e-3 * max(abs(r64["payoffValues"][0]), 1e-3)
+
+
+@pytest.mark.parametrize("steps", [1, 2, 3])
+@pytest.mark.parametrize("prod", ["uoc", "european"])
+def test_fp32_risk_kernel_short_timelines(eng, steps, prod):
+    """Timelines of one to three steps (the reverse sweep's loads run ahead of the step it
+    computes): FP32 against FP64 on the same paths, within FP32 rounding of the path
+    arithmetic."""
+    from compfinance_gb300 import workloads as W
+    s, t, v = W.dupire_surface(60, 30)
+    eng.putDupire(W.DUPIRE_SPOT, s, t, v, W.DUPIRE_MAXDT, "short60")
+    T = (steps - 0.5) * W.DUPIRE_MAXDT
+    if prod == "uoc":
+        eng.putBarrier(100.0, 104.0, T, T / steps, 0.01, 0, "short_p")
+    else:
+        eng.putEuropean(100.0, T, T, "short_p")
+    assert eng.shapes("short60", "short_p")[2] == steps
+    for sob in (0, 1):
+        r64 = eng.AADriskOne("short60", "short_p", num(sob, 4096, "fp64"))
+        r32 = eng.AADriskOne("short60", "short_p", num(sob, 4096, "fp32"))
+        scale = max(np.abs(r64["risks"]).max(), 1e-3)
+        assert np.abs(r64["risks"]).max() > 0
+        assert np.abs(r32["risks"] - r64["risks"]).max() <= 5e-3 * scale, (steps, prod, sob)
+        assert abs(r32["payoffValues"][0] - r64["payoffValues"][0]) <= 1e-3 * max(abs(r64["payoffValues"][0]), 1e-3)

@@ -140,7 +140,7 @@ __global__ void __launch_bounds__(RB, 8) dupire_risk32(const McParams p)
     const float spot = (float)p.spot;
     const float w0 = nPay > 0 ? p.wf[0] : 0.0f, w1 = nPay > 1 ? p.wf[1] : 0.0f;
     const float bX0 = p.bX0F, bInvW = p.bInvWF;
-    const int nB = p.nBucketsF;
+    const float bMaxF = float(p.nBucketsF - 1);
 
     // scratch [ring slot][field][point][thread], 32-bit offsets (the host keeps it below 2^31
     // elements).  Point nSteps of a path's step-word field holds its adjoint seed, and point
@@ -172,9 +172,7 @@ __global__ void __launch_bounds__(RB, 8) dupire_risk32(const McParams p)
     // upper_bound of xs among the knots (exact: a bucket holds at most one knot, and the
     // bucket of xs computed in FP32 is off by at most one)
     auto search = [&](float xs) -> int {
-        const float fb = (xs - bX0) * bInvW;
-        int b = 0;
-        if (fb > 0.0f) b = fb < float(nB - 1) ? int(fb) : nB - 1;
+        const int b = __float2int_rz(fminf(fmaxf((xs - bX0) * bInvW, 0.0f), bMaxF));  // NaN -> 0
         const int l0 = sBucket[b];
         const int lo = l0 + (sXs[l0 + 1] <= xs ? 1 : 0) - (sXs[l0] > xs ? 1 : 0);
         return lo < nS ? lo : nS;  // +inf would pass the last sentinel

@@ -714,7 +714,7 @@ int Context::getPlan(const std::string& mid, const std::string& pid, Plan*& out)
         out = it->second.get();
         return CF_OK;
     }
-    auto plan = std::make_unique<Plan>();
+    auto plan = std::make_shared<Plan>();
     if (it != plans.end())
     {
         // the model or product changed: the new plan takes over the stale plan's device tables
@@ -855,6 +855,7 @@ int Context::enqueue(Slot& slot, Plan& plan, const cf_num_param& num, bool risk,
     CF_CUDA(cudaEventRecord(slot.done, st));
     slot.last = p;
     slot.plan = &plan;
+    slot.planRef = plan.weak_from_this().lock();
     slot.risk = risk;
     slot.multi = false;
     slot.launches = 1;

@@ -98,7 +98,7 @@ struct ProductDesc
 
 
 // The device tables of one (model, product) pair.
-struct Plan
+struct Plan : std::enable_shared_from_this<Plan>
 {
     int model = 0, prod = 0, nSteps = 0, nEv = 0, nPay = 0, nParam = 0;
     bool sobolOk = false;
@@ -140,6 +140,9 @@ struct Slot
     cudaEvent_t done = nullptr;
     McParams last;
     Plan* plan = nullptr;
+    // keeps the plan of the last run alive (its host data is read when the results are
+    // fetched) even if the store replaces it meanwhile; empty for plans the store does not own
+    std::shared_ptr<Plan> planRef;
     bool risk = false, multi = false;
     int launches = 0;
     // multi-risk bookkeeping (strike buckets, see multi.cpp)
@@ -160,7 +163,7 @@ struct Context
     unsigned long long versionCounter = 0;
     std::map<std::string, ModelDesc> models;
     std::map<std::string, ProductDesc> products;
-    std::map<std::pair<std::string, std::string>, std::unique_ptr<Plan>> plans;
+    std::map<std::pair<std::string, std::string>, std::shared_ptr<Plan>> plans;
     DevBuf jump;
     const unsigned long long* jumpA = nullptr;
     const unsigned long long* jumpB = nullptr;

@@ -215,6 +215,7 @@ int Context::enqueueMulti(Slot& slot, Plan& plan, const cf_num_param& num, doubl
     if (e) return cuda_fail(e, "multi download");
     d2h += riskBytes + slot.accVBytes + 4;
     slot.plan = &plan;
+    slot.planRef = plan.weak_from_this().lock();
     slot.multi = true;
     slot.risk = true;
     slot.multiParams = nParam;

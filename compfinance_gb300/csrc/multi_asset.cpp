@@ -363,6 +363,7 @@ int Context::enqueueMd(Slot& slot, Plan& plan, const cf_num_param& num, bool ris
     CF_CUDA(cudaEventRecord(slot.done, st));
     slot.last = p;
     slot.plan = &plan;
+    slot.planRef = plan.weak_from_this().lock();
     slot.risk = risk;
     slot.multi = false;
     slot.launches = 1;

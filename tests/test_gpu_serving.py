@@ -85,3 +85,35 @@ def test_cancel_and_queue_timeout(eng):
     assert srv.wait(first) == "done"
     assert srv.wait(t) in ("timeout", "done")
     srv.close()
+
+
+def test_model_replaced_while_requests_run(eng):
+    """A model re-put while requests on it run: requests that started run on the model as it
+    was when they started, requests that start later on the new one.  The replaced plan stays
+    valid until its results have been fetched (the new plan takes over its device tables)."""
+    import time
+    s, t, v = W.dupire_surface(60, 30)
+    u = W.UOC_BARRIER
+    eng.putBarrier(u["strike"], u["barrier"], u["maturity"], u["monitor_freq"], u["smooth"], 0, "rp_uoc")
+    num = NumericalParam(numPath=1 << 18, precision="fp32")
+    eng.putDupire(W.DUPIRE_SPOT, s, t, v * 1.1, W.DUPIRE_MAXDT, "rp_dup")
+    new = eng.AADriskOne("rp_dup", "rp_uoc", num)
+    eng.putDupire(W.DUPIRE_SPOT, s, t, v, W.DUPIRE_MAXDT, "rp_dup")
+    old = eng.AADriskOne("rp_dup", "rp_uoc", num)
+    assert not np.array_equal(old["risks"], new["risks"])
+    srv = Server(eng, slots=2, hbm_budget=64 << 30)
+    ids = [srv.submit("risk", "rp_dup", "rp_uoc", num) for _ in range(2)]
+    t0 = time.time()
+    while any(srv.wait(i, timeout_ms=0) == "queued" for i in ids):
+        assert time.time() - t0 < 30
+        time.sleep(0.0005)
+    eng.putDupire(W.DUPIRE_SPOT, s, t, v * 1.1, W.DUPIRE_MAXDT, "rp_dup")
+    later = srv.submit("risk", "rp_dup", "rp_uoc", num)  # lowers the new plan when it starts
+    assert srv.wait(later) == "done"
+    for i in ids:
+        assert srv.wait(i) == "done"
+        got = srv.result(i)
+        assert np.array_equal(got["risks"], old["risks"]) and np.array_equal(got["values"], old["payoffValues"])
+    got = srv.result(later)
+    assert np.array_equal(got["risks"], new["risks"]) and np.array_equal(got["values"], new["payoffValues"])
+    srv.close()

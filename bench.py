@@ -35,7 +35,8 @@ METRIC = "AAD-risk paths/s (Dupire barrier), FP32 vs FP64 at equal error; serve 
 NPATH = 1 << 22
 GRID = (60, 30)
 FLOPS_PER_PATH_STEP = 53.0   # algorithmic FP work of value + adjoint per path-step (mrg32k3a)
-TRAFFIC_BYTES_PER_PATH_STEP = 11.34  # measured DRAM traffic of the FP32 risk launch per path-step
+TRAFFIC_BYTES_PER_PATH_STEP = 11.73  # measured DRAM traffic of the FP32 risk launch per path-step
+INST_PER_PATH_STEP = 117.7  # measured thread instructions of the FP32 risk launch per path-step
 CONFIG = {
     "workload": "dupire_uoc_aad_risk_60x30_156steps_2^22paths_fp32path",
     "model": "Dupire local vol 60x30 (50-200 log-spaced x 0.1-3.0y), seeded synthetic surface",
@@ -499,7 +500,14 @@ def main():
                      # reverse-sweep scratch) over the launch time, of the measured copy bandwidth
                      "hbm": ({"achieved_gbs": traffic / per_step / 1e9, "peak_gbs": pk.get("hbm_gbs"),
                               "frac": traffic / per_step / 1e9 / pk["hbm_gbs"]}
-                             if traffic and pk.get("hbm_gbs") else None)},
+                             if traffic and pk.get("hbm_gbs") else None),
+                     # and against instruction issue, its actual bound: thread instructions per
+                     # path-step (smsp__inst_executed x active lanes, same ncu capture) over the
+                     # launch time, of 152 SMs x 4 schedulers x 32 lanes x sm_max_mhz
+                     "issue": {"achieved_tinst_per_s": INST_PER_PATH_STEP * steps_tot / per_step,
+                               "peak_tinst_per_s": 152 * 4 * 32 * sm_max * 1e6,
+                               "frac": INST_PER_PATH_STEP * steps_tot / per_step / (152 * 4 * 32 * sm_max * 1e6),
+                               "inst_per_path_step": INST_PER_PATH_STEP}},
         "e2e": {"value": world * npath / e2e_t, "unit": "paths/s", "h2d_bytes_per_step": (h1 - h0) // ke,
                 "d2h_bytes_per_step": (d1 - d0) // ke},
         "gpu_launches": launches,

@@ -165,7 +165,7 @@ struct McParams
     int fast32;           // 1 when the plan carries these tables (the launch may use the kernel)
     const float* xsF;     // [nS + 2] knots with -inf / +inf sentinels at both ends
     const float* irF;     // [nS + 1][2] (xr, ir) per interval
-    const float* tdF;     // [nSteps][nS + 1][2] (y, d) per step and interval
+    const float* tdF;     // [nSteps][nS + 1][2] (y - 2 d, d) per step and interval
     const int* bucketF;   // [nBucketsF] upper_bound of each bucket's left edge; buckets are
                           // narrower than 2/3 of the smallest knot spacing (at most one knot each)
     int nBucketsF;

@@ -525,11 +525,14 @@ int Context::buildPlan(const ModelDesc& m, const ProductDesc& pd, Plan& plan)
             {
                 const double* y = &Y[size_t(i) * nS];
                 float* o = &tdv[2 * size_t(i) * (nS + 1)];
+                // (y - 2 d, d): the kernels evaluate y + d t as (y - 2 d) + d (t + 2) straight from
+                // the quantised float t + 2
                 o[0] = float(y[0]);
                 for (int lo = 1; lo < nS; ++lo)
                 {
-                    o[2 * lo] = float(y[lo - 1]);
-                    o[2 * lo + 1] = float(y[lo] - y[lo - 1]);
+                    const double d = y[lo] - y[lo - 1];
+                    o[2 * lo] = float(y[lo - 1] - 2.0 * d);
+                    o[2 * lo + 1] = float(d);
                 }
                 o[2 * nS] = float(y[nS - 1]);
             }

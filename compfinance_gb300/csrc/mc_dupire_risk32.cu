@@ -262,14 +262,17 @@ __global__ void __launch_bounds__(RB, (PROD == PROD_UOC && RNGK == RNG_SOBOL) ? 
                 const float t2 = fminf((x[a] - ir.x) * ir.y, T_MAX) + 2.0f;
                 const unsigned tq = __float_as_uint(t2) & T_MASK;
                 const float2 yd = __ldg(trow + lo);
-                const float v = fmaf(yd.y, t2 - 2.0f, yd.x);
+                const float v = fmaf(yd.y, t2, yd.x);  // table (y - 2 d, d)
                 __stcs(reinterpret_cast<unsigned*>(fs) + (F_W + a) * rowStride + s * Ti + myCol,
                        (unsigned(lo) << LO_SHIFT) | flag[a] | tq);
                 flag[a] = 0;  // the flag of point s + 1 is set by its date, if any
                 x[a] += v * (-0.5f * v + ga);
             }
-            // the barrier monitors at dates only; a European's one date is the last point
-            if (UOC ? (evEvery || __ldg(p.evAtStep + s + 1) >= 0) : s + 1 == nSteps)
+            // the barrier monitors at dates only (and a date below the band needs nothing before
+            // maturity: one test for both paths of the pair); a European's one date is the last point
+            if (UOC ? (evEvery || __ldg(p.evAtStep + s + 1) >= 0) &&
+                          (s + 1 == nSteps || fmaxf(x[0], x[NP - 1]) > logBand)
+                    : s + 1 == nSteps)
 #pragma unroll
                 for (int a = 0; a < NP; ++a)
                     if (a < nAct) event(s + 1, a);
@@ -426,8 +429,8 @@ __global__ void __launch_bounds__(RB, (PROD == PROD_UOC && RNGK == RNG_SOBOL) ? 
                 }
                 const float ga = a ? -g1 : g1;
                 const int lo = int(W >> LO_SHIFT);
-                const float t = __uint_as_float(TWO_BITS | (W & T_MASK)) - 2.0f;
-                const float v = fmaf(yd.y, t, yd.x);
+                const float t2 = __uint_as_float(TWO_BITS | (W & T_MASK)), t = t2 - 2.0f;
+                const float v = fmaf(yd.y, t2, yd.x);  // the forward's expression
                 const float av = ax * (ga - v);      // d x_{s+1} / d v = g - v
                 ax += av * (yd.y * ir.y);            // d x_{s+1} / d x_s = 1 + (g - v) dv/dx
                 if (av != 0.0f)

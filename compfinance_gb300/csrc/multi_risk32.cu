@@ -204,7 +204,7 @@ __global__ void __launch_bounds__(MB) multi32_forward(const Multi32Args A)
                 const float t2 = fminf((x[a] - ir.x) * ir.y, T_MAX) + 2.0f;
                 const unsigned tq = __float_as_uint(t2) & T_MASK;
                 const float2 yd = __ldg(trow + lo);
-                const float v = fmaf(yd.y, t2 - 2.0f, yd.x);
+                const float v = fmaf(yd.y, t2, yd.x);  // table (y - 2 d, d)
                 const uint2 r = make_uint2((unsigned(lo) << LO_SHIFT) | tq, __float_as_uint(ga));
                 // records are written in pairs of steps (one 16-byte store)
                 if (s & 1)
@@ -431,10 +431,10 @@ __global__ void __launch_bounds__(MB) multi32_reverse(const Multi32Args A)
             auto step = [&](int s, unsigned W, unsigned gbits) {
                 const float ga = __uint_as_float(gbits);
                 const int l = int(W >> LO_SHIFT);
-                const float t = __uint_as_float(TWO_BITS | (W & T_MASK)) - 2.0f;
+                const float t2 = __uint_as_float(TWO_BITS | (W & T_MASK)), t = t2 - 2.0f;
                 const float2 yd = __ldg(td + size_t(s) * tPitch + l);
                 const float2 ir = sIr[l];
-                const float v = fmaf(yd.y, t, yd.x);
+                const float v = fmaf(yd.y, t2, yd.x);  // the forward's expression
                 const float av = ax * (ga - v);  // d x_{s+1} / d v = g - v
                 ax += av * (yd.y * ir.y);        // d x_{s+1} / d x_s = 1 + (g - v) dv/dx
                 if (av == 0.0f) return;

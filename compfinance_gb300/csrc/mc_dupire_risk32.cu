@@ -17,15 +17,17 @@
 //  3. reverse: while 128 paths are pending, the block sweeps a chunk of 128 (one path per
 //     thread, every thread busy); a partial chunk runs only when the oldest pending paths'
 //     slot is about to be rewritten, and once at the end.  Each listed path is swept back
-//     from maturity to today by one thread, with no block barrier inside the sweep.  The adjoint of each local-vol value the step used is
-//     split over its two spot knots and, with the step's time weights, over its two time
-//     columns, and each of the (up to) four parts is rounded once to an integer in units of
-//     2^-nodeShiftF and added (native 32-bit shared atomics) to an int32 slab of the
-//     local-vol nodes.  The host picks nodeShiftF so that no slab word can overflow within
-//     256 paths; after each chunk (at most 128 paths) the slab is moved into a block-private
-//     int64 slab in global memory (each word owned by one thread), which is added to the
-//     accumulators once, at the end.  Each contribution is rounded once, so every sum is independent of
-//     how paths are grouped into warps, blocks and launches.
+//     from maturity to today by one thread, with no block barrier inside the sweep.  The
+//     adjoint of each local-vol value the step used is split over its two spot knots and,
+//     with the step's time weights, over its two time columns.  Each of the (up to) four
+//     parts is rounded once to an integer in units of 2^-nodeShiftF and added (native 32-bit
+//     shared atomics) to an int32 slab of the local-vol nodes; parts of large adjoints go, in
+//     the same unit, to a block-private int64 slab in global memory (64-bit atomics).  The
+//     host picks nodeShiftF so that no int32 word can overflow within 256 paths; after each
+//     chunk (at most 128 paths) the int32 slab is moved into the int64 slab, whose words are
+//     added to the accumulators once, at the end.  Each contribution is rounded once, so
+//     every sum is independent of how paths are grouped into warps, blocks, chunks and
+//     launches.
 #include <cuda_runtime.h>
 
 #include "cf_device.cuh"

@@ -254,3 +254,24 @@ def test_fp32_risk_kernel_short_timelines(eng, steps, prod):
         assert np.abs(r64["risks"]).max() > 0
         assert np.abs(r32["risks"] - r64["risks"]).max() <= 5e-3 * scale, (steps, prod, sob)
         assert abs(r32["payoffValues"][0] - r64["payoffValues"][0]) <= 1e-3 * max(abs(r64["payoffValues"][0]), 1e-3)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_tma_staged_local_vols_bit_identical(eng, monkeypatch, precision):
+    """The generic kernel's local-vol table staged into shared memory by a TMA bulk copy
+    (cp.async.bulk with an mbarrier, forced by CF_STAGE_Y=1) and read through L1 instead
+    (CF_STAGE_Y=0): the same numbers bit for bit, and no device error flag (the bounded wait
+    on the copy did not run out).  CF_FAST32=0 keeps FP32 risk on the generic kernel."""
+    from compfinance_gb300 import workloads as W
+    s, t, v = W.dupire_surface(60, 30)
+    u = W.UOC_BARRIER
+    eng.putDupire(W.DUPIRE_SPOT, s, t, v, W.DUPIRE_MAXDT, "tma60")
+    eng.putBarrier(u["strike"], u["barrier"], u["maturity"], u["monitor_freq"], u["smooth"], 0, "tma_p")
+    monkeypatch.setenv("CF_FAST32", "0")
+    out = {}
+    for stage in ("1", "0"):
+        monkeypatch.setenv("CF_STAGE_Y", stage)
+        out[stage] = eng.AADriskOne("tma60", "tma_p", num(0, 1 << 15, precision))
+    assert np.array_equal(out["1"]["payoffValues"], out["0"]["payoffValues"])
+    assert np.array_equal(out["1"]["risks"], out["0"]["risks"])
+    assert np.abs(out["1"]["risks"]).max() > 0

@@ -515,17 +515,27 @@ def main():
         "clocks": clocks,
         "step_ms": [round(x, 4) for x in ms32],
     }
+    def leg(key, fn, *a, **k):
+        """An auxiliary measurement: a failure is reported in the line, not fatal to it."""
+        try:
+            out[key] = fn(*a, **k)
+        except Exception as e:  # noqa: BLE001
+            out[key] = {"error": f"{type(e).__name__}: {e}"}
+
     if not args.no_sweep:
-        out["grid_sweep"] = grid_sweep(eng, stream, flush, npath)
-        out["superbucket"] = superbucket_leg(eng)
-        out["bump_risk"] = bump_leg(eng)
-        out["multi_asset"] = multi_asset_leg(eng)
+        leg("grid_sweep", grid_sweep, eng, stream, flush, npath)
+        leg("superbucket", superbucket_leg, eng)
+        leg("bump_risk", bump_leg, eng)
+        leg("multi_asset", multi_asset_leg, eng)
     if not args.no_serving:
-        out["serving"] = serving_leg(eng, args.serve_requests, seed=2026 + rank)
+        leg("serving", serving_leg, eng, args.serve_requests, seed=2026 + rank)
     if rank == 0 and not args.no_cpu:
-        out["cpu_baseline"] = cpu_baseline()
-        if "multi_asset" in out:
-            out["multi_asset"]["cpu_baseline"] = cpu_multi_asset()
+        leg("cpu_baseline", cpu_baseline)
+        if "multi_asset" in out and "error" not in out["multi_asset"]:
+            try:
+                out["multi_asset"]["cpu_baseline"] = cpu_multi_asset()
+            except Exception as e:  # noqa: BLE001
+                out["multi_asset"]["cpu_baseline"] = {"error": f"{type(e).__name__}: {e}"}
     if rank == 0:
         print(json.dumps(out))
     eng.close()

@@ -168,6 +168,7 @@ struct McParams
     const float* tdF;     // [nSteps][nS + 1][2] (y - 2 d, d) per step and interval
     const int* bucketF;   // [nBucketsF] upper_bound of each bucket's left edge; buckets are
                           // narrower than 2/3 of the smallest knot spacing (at most one knot each)
+                          // and, for dupire_risk32, no knot lies near an edge
     int nBucketsF;
     float bX0F, bInvWF;
     // Node adjoints are rounded to units of 2^-nodeShiftF (<= FIX_HI_SHIFT), chosen per plan so

@@ -536,19 +536,8 @@ int Context::buildPlan(const ModelDesc& m, const ProductDesc& pd, Plan& plan)
                 }
                 o[2 * nS] = float(y[nS - 1]);
             }
-            double minGap = INFINITY;
-            for (int j = 0; j + 1 < nS; ++j) minGap = std::min(minGap, double(Xf[j + 1]) - double(Xf[j]));
-            const double range = nS > 1 ? double(Xf[nS - 1]) - double(Xf[0]) : 0.0;
-            int nBf = 8;
-            while (nBf < 4096 && range / nBf > minGap / 1.5) nBf *= 2;
-            const double wf = range > 0 ? range / nBf : 1.0;
-            std::vector<int> bf(nBf);
-            for (int b = 0; b < nBf; ++b)
-            {
-                const double edge = double(Xf[0]) + b * wf;
-                bf[b] = int(std::upper_bound(Xf.begin(), Xf.end(), edge,
-                                             [](double e, float x) { return e < double(x); }) - Xf.begin());
-            }
+            const BucketGrid bg = bucket_grid(Xf);
+            const std::vector<int>& bf = bg.first;
             bool evOk = evAtStep[n] == plan.nEv - 1;
             if (pd.kind == PROD_EUROPEAN)
                 for (int i = 0; i < n; ++i) evOk = evOk && evAtStep[i] < 0;
@@ -559,15 +548,14 @@ int Context::buildPlan(const ModelDesc& m, const ProductDesc& pd, Plan& plan)
             const double perWord = 256.0 * sMax * 512.0 * std::max(wMax, 1e-300);
             const int shift = int(std::floor(std::log2(1073741824.0 / perWord)));  // one bit of margin
             P.nodeShiftF = std::min(FIX_HI_SHIFT, shift);
-            P.fast32 = (pd.kind == PROD_UOC || pd.kind == PROD_EUROPEAN) && evOk && nS <= 510 && minGap > 0 &&
-                       range / nBf <= minGap / 1.5 && shift >= 4;
+            P.fast32 = (pd.kind == PROD_UOC || pd.kind == PROD_EUROPEAN) && evOk && nS <= 510 && bg.ok &&
+                       bg.oneCompare && shift >= 4;
             // FP32 AADriskMulti (multi_risk32.cu) uses the same tables and slab unit: its chunks
             // hold 256 paths of one bucket
-            plan.multi32 = pd.kind == PROD_EUROPEANS && nS <= 510 && minGap > 0 && range / nBf <= minGap / 1.5 &&
-                           shift >= 4;
-            P.nBucketsF = nBf;
-            P.bX0F = Xf[0];
-            P.bInvWF = float(1.0 / wf);
+            plan.multi32 = pd.kind == PROD_EUROPEANS && nS <= 510 && bg.ok && shift >= 4;
+            P.nBucketsF = int(bf.size());
+            P.bX0F = bg.x0;
+            P.bInvWF = bg.invW;
             oXs = pk.vec(xs);
             oIr = pk.vec(irv);
             oTd = pk.vec(tdv);
@@ -1005,6 +993,26 @@ int cf_last_error(char* buf, size_t size)
 {
     if (!buf || !size) return CF_E_ARG;
     std::snprintf(buf, size, "%s", g_lastError.c_str());
+    return CF_OK;
+}
+
+int cf_bucket_grid(const float* knots, int nKnots, int capacity, float* x0, float* invW, int* nBuckets, int* ok,
+                   int* oneCompare, int* first)
+{
+    if (!knots || nKnots < 1 || !nBuckets) return fail(CF_E_ARG, "bucket grid: null argument or no knots");
+    for (int j = 0; j + 1 < nKnots; ++j)
+        if (!(knots[j] < knots[j + 1])) return fail(CF_E_ARG, "bucket grid: knots not strictly ascending");
+    const BucketGrid g = bucket_grid(std::vector<float>(knots, knots + nKnots));
+    *nBuckets = int(g.first.size());
+    if (x0) *x0 = g.x0;
+    if (invW) *invW = g.invW;
+    if (ok) *ok = g.ok ? 1 : 0;
+    if (oneCompare) *oneCompare = g.oneCompare ? 1 : 0;
+    if (first)
+    {
+        if (capacity < *nBuckets) return fail(CF_E_SHAPE, "bucket grid: capacity below the bucket count");
+        std::copy(g.first.begin(), g.first.end(), first);
+    }
     return CF_OK;
 }
 

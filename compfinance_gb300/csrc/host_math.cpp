@@ -247,4 +247,70 @@ void inv_normal_table(double denom, float* out)
         }
 }
 
+BucketGrid bucket_grid(const std::vector<float>& X)
+{
+    BucketGrid g;
+    const int nS = int(X.size());
+    if (nS < 1) return g;
+    double minGap = INFINITY;
+    for (int j = 0; j + 1 < nS; ++j) minGap = std::min(minGap, double(X[j + 1]) - double(X[j]));
+    const double range = nS > 1 ? double(X[nS - 1]) - double(X[0]) : 0.0;
+    int nBf = 8;
+    while (nBf < 4096 && range / nBf > minGap / 1.5) nBf *= 2;
+    g.ok = nS > 1 && minGap > 0 && range / nBf <= minGap / 1.5;
+    // default grid: nBf buckets from the first knot
+    const double wDefault = range > 0 ? range / nBf : 1.0;
+    g.x0 = X[0];
+    g.invW = float(1.0 / wDefault);
+    int nB = nBf;
+    double w = wDefault;
+    if (g.ok)
+    {
+        // counts 2 (nS - 1) and 3 (nS - 1) put every knot of an evenly spaced grid at the same
+        // place in its bucket; then the power of two and a run of counts above the smallest
+        std::vector<int> cands = {2 * (nS - 1), 3 * (nS - 1), nBf};
+        const int n0 = std::max(8, int(std::ceil(1.5 * range / minGap)));
+        for (int k = 0; k < 48; ++k) cands.push_back(n0 + k);
+        for (size_t c = 0; c < cands.size() && !g.oneCompare; ++c)
+        {
+            const int N = cands[c];
+            if (N < 8 || N > 4096) continue;
+            const float iw = float(1.0 / (range / N));
+            const double Wd = 1.0 / double(iw);  // the width the kernel's FP32 index uses
+            if (Wd > minGap / 1.5) continue;
+            for (double off : {0.5, 0.25, 0.75, 0.125, 0.375, 0.625, 0.875})
+            {
+                const float b0 = float(double(X[0]) - off * Wd);
+                // two buckets past the last knot: a state above it finds no knot to compare
+                const int nb = int(std::ceil((double(X[nS - 1]) - double(b0)) / Wd)) + 2;
+                const double eps =
+                    8.0 * std::ldexp(1.0, -23) * (double(X[nS - 1]) - double(b0) + 2.0 * Wd + std::fabs(double(b0)));
+                bool fits = Wd > 10.0 * eps && nb <= 4098;
+                for (int j = 0; fits && j < nS; ++j)
+                {
+                    const double u = (double(X[j]) - double(b0)) / Wd;
+                    fits = std::min(u - std::floor(u), std::ceil(u) - u) * Wd >= eps;
+                }
+                if (fits)
+                {
+                    g.x0 = b0;
+                    g.invW = iw;
+                    nB = nb;
+                    w = Wd;
+                    g.oneCompare = true;
+                    break;
+                }
+            }
+        }
+    }
+    g.first.resize(size_t(nB));
+    for (int b = 0; b < nB; ++b)
+    {
+        const double edge = double(g.x0) + b * w;
+        g.first[size_t(b)] =
+            int(std::upper_bound(X.begin(), X.end(), edge, [](double e, float x) { return e < double(x); }) - X.begin());
+    }
+    return g;
+}
+
 }  // namespace cf

@@ -47,6 +47,22 @@ constexpr int INVN_SUB_BITS = 4;
 constexpr int INVN_PIECES = 32 << INVN_SUB_BITS;
 void inv_normal_table(double denom, float* out /* [INVN_PIECES][4] */);
 
+// Equal buckets over the log-spot knots of the FP32 Dupire kernels: bucket b is
+// [x0 + b / invW, x0 + (b + 1) / invW) and first[b] the index of the first knot above its left
+// edge (the upper_bound of the edge).  ok: every bucket holds at most one knot (buckets
+// narrower than 2/3 of the smallest knot spacing, at most 4096 of them).  oneCompare: besides,
+// no knot lies within eps = 8 x 2^-23 x the span of a bucket edge, so the bucket index of a
+// state x computed in FP32, (x - x0) invW, is exact or one off next to an edge with no knot
+// near; then upper_bound(x) = first[b] + (knot first[b] <= x), one comparison.  Without
+// oneCompare the grid is the default one (from the first knot), searched with two comparisons.
+struct BucketGrid
+{
+    bool ok = false, oneCompare = false;
+    float x0 = 0.0f, invW = 1.0f;
+    std::vector<int> first;
+};
+BucketGrid bucket_grid(const std::vector<float>& knots);
+
 // Black-Scholes formula, Zelen-Severo normal CDF, implied vol, Merton (analytics.h:8-91).
 double normal_cdf(double x);
 double normal_dens(double x);

@@ -175,12 +175,14 @@ __global__ void __launch_bounds__(RB, (PROD == PROD_UOC && RNGK == RNG_SOBOL) ? 
         return sup ? -g : g;
     };
 
-    // upper_bound of xs among the knots (exact: a bucket holds at most one knot, and the
-    // bucket of xs computed in FP32 is off by at most one)
+    // upper_bound of xs among the knots: a bucket holds at most one knot, and the host placed
+    // the buckets so that no knot lies near an edge, where the FP32 bucket index can be one off;
+    // so xs lies above the knot below the bucket's first interval, and only the knot above it
+    // needs a comparison
     auto search = [&](float xs) -> int {
         const int b = __float2int_rz(fminf(fmaxf((xs - bX0) * bInvW, 0.0f), bMaxF));  // NaN -> 0
         const int l0 = sBucket[b];
-        const int lo = l0 + (sXs[l0 + 1] <= xs ? 1 : 0) - (sXs[l0] > xs ? 1 : 0);
+        const int lo = l0 + (sXs[l0 + 1] <= xs ? 1 : 0);
         return lo < nS ? lo : nS;  // +inf would pass the last sentinel
     };
 

@@ -303,6 +303,15 @@ int cf_server_reset_stats(cf_server* server);
 /* Test hook: the next n request starts fail as if a device allocation had failed. */
 int cf_server_inject_failures(cf_server* server, int startFailures);
 
+/* Test hook, no device call: the equal-width buckets over a Dupire model's log-spot knots
+ * (ascending floats) that the FP32 kernels search, no counterpart in the reference.  Bucket b
+ * is [x0 + b / invW, x0 + (b + 1) / invW); first[b] is the index of the first knot above its
+ * left edge.  ok = 1: every bucket holds at most one knot.  oneCompare = 1: besides, no knot
+ * lies near a bucket edge, so the FP32 risk kernel finds a state's interval with one
+ * comparison (it runs only on such grids).  first == NULL queries *nBuckets only. */
+int cf_bucket_grid(const float* knots, int nKnots, int capacity, float* x0, float* invW, int* nBuckets, int* ok,
+                   int* oneCompare, int* first);
+
 #ifdef __cplusplus
 }
 #endif

@@ -35,8 +35,8 @@ METRIC = "AAD-risk paths/s (Dupire barrier), FP32 vs FP64 at equal error; serve 
 NPATH = 1 << 22
 GRID = (60, 30)
 FLOPS_PER_PATH_STEP = 53.0   # algorithmic FP work of value + adjoint per path-step (mrg32k3a)
-TRAFFIC_BYTES_PER_PATH_STEP = 11.73  # measured DRAM traffic of the FP32 risk launch per path-step
-INST_PER_PATH_STEP = 117.7  # measured thread instructions of the FP32 risk launch per path-step
+TRAFFIC_BYTES_PER_PATH_STEP = 11.79  # measured DRAM traffic of the FP32 risk launch per path-step
+INST_PER_PATH_STEP = 107.5  # measured thread instructions of the FP32 risk launch per path-step
 CONFIG = {
     "workload": "dupire_uoc_aad_risk_60x30_156steps_2^22paths_fp32path",
     "model": "Dupire local vol 60x30 (50-200 log-spaced x 0.1-3.0y), seeded synthetic surface",

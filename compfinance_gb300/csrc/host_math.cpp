@@ -252,6 +252,14 @@ BucketGrid bucket_grid(const std::vector<float>& X)
     BucketGrid g;
     const int nS = int(X.size());
     if (nS < 1) return g;
+    if (nS == 1)  // local vol flat in spot: unit buckets, the knot in the middle of the first
+    {
+        g.ok = g.oneCompare = true;
+        g.x0 = X[0] - 0.5f;
+        g.invW = 1.0f;
+        g.first = {0, 1, 1};
+        return g;
+    }
     double minGap = INFINITY;
     for (int j = 0; j + 1 < nS; ++j) minGap = std::min(minGap, double(X[j + 1]) - double(X[j]));
     const double range = nS > 1 ? double(X[nS - 1]) - double(X[0]) : 0.0;

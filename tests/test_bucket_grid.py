@@ -56,6 +56,7 @@ def probe_points(knots, x0, iw, nb, rs):
 def knot_sets():
     rs = np.random.RandomState(5)
     sets = [W.dupire_surface(*g)[0] for g in ((20, 10), (60, 30), (120, 60))]
+    sets += [np.array([100.0]), np.array([73.0])]  # one knot: local vol flat in spot
     sets += [50.0 * 4.0 ** (np.arange(n) / (n - 1)) for n in (2, 3, 7, 60, 121, 350, 510)]  # log-spaced
     sets += [np.linspace(50.0, 200.0, n) for n in (5, 60, 255, 500)]  # evenly spaced in spot
     sets += [np.sort(rs.uniform(40.0, 250.0, n)) for n in (5, 17, 60, 200) for _ in range(5)]

@@ -275,3 +275,26 @@ def test_tma_staged_local_vols_bit_identical(eng, monkeypatch, precision):
     assert np.array_equal(out["1"]["payoffValues"], out["0"]["payoffValues"])
     assert np.array_equal(out["1"]["risks"], out["0"]["risks"])
     assert np.abs(out["1"]["risks"]).max() > 0
+
+
+@pytest.mark.parametrize("prod", ["uoc", "european"])
+def test_fp32_risk_kernel_one_spot_knot(eng, prod):
+    """A local vol flat in spot (one spot knot, 30 times): the FP32 risk kernel against FP64 on
+    the same paths, within FP32 rounding of the path arithmetic."""
+    from compfinance_gb300 import workloads as W
+    s, t, v = W.dupire_surface(60, 30)
+    vols = np.asarray(v).reshape(len(s), len(t))[30:31, :]  # the row of spot ~100, [1][nT]
+    eng.putDupire(W.DUPIRE_SPOT, np.array([100.0]), t, vols, W.DUPIRE_MAXDT, "flat1")
+    u = W.UOC_BARRIER
+    if prod == "uoc":
+        eng.putBarrier(u["strike"], u["barrier"], u["maturity"], u["monitor_freq"], u["smooth"], 0, "flat_p")
+    else:
+        eng.putEuropean(110.0, 2.0, 2.0, "flat_p")
+    assert eng.shapes("flat1", "flat_p")[1] == 1 + len(t)
+    for sob in (0, 1):
+        r64 = eng.AADriskOne("flat1", "flat_p", num(sob, 1 << 14, "fp64"))
+        r32 = eng.AADriskOne("flat1", "flat_p", num(sob, 1 << 14, "fp32"))
+        scale = np.abs(r64["risks"]).max()
+        assert scale > 0
+        assert np.abs(r32["risks"] - r64["risks"]).max() <= 5e-3 * scale, (prod, sob)
+        assert abs(r32["payoffValues"][0] - r64["payoffValues"][0]) <= 1e-3 * max(abs(r64["payoffValues"][0]), 1e-3)

@@ -45,7 +45,7 @@ CONFIG = {
     "paths": NPATH,
     "risks": 1801,
     "l2": "flushed between steps (256 MiB write outside the per-step events); the reverse-sweep scratch "
-          "(three unit-round slots, ~2 GB) also exceeds L2",
+          "(three unit-round slots, ~2.3 GB) also exceeds L2",
 }
 
 
@@ -116,10 +116,14 @@ def _cpu_case():
 def _cpu_sample_size(O, m, p, w, threads, seconds):
     """Paths (even) that the threaded CPU adjoint runs in about `seconds`."""
     n = 1 << 12
-    t0 = time.perf_counter()
-    O.risk(m, p, 0, n, w, fast=True, threads=threads)
-    dt = time.perf_counter() - t0
-    n = int(min(1 << 23, max(n, n * seconds / max(dt, 1e-3))))
+    while True:  # a calibration run long enough that thread start-up does not dominate it
+        t0 = time.perf_counter()
+        O.risk(m, p, 0, n, w, fast=True, threads=threads)
+        dt = time.perf_counter() - t0
+        if dt >= 0.5 or n >= 1 << 22:
+            break
+        n *= 4
+    n = int(min(1 << 25, max(n, n * seconds / max(dt, 1e-3))))
     return n - n % 2
 
 

@@ -127,7 +127,7 @@ def _cpu_sample_size(O, m, p, w, threads, seconds):
     return n - n % 2
 
 
-def cpu_baseline(seconds=12.0, threads=None):
+def cpu_baseline(seconds=18.0, threads=None):
     """The oracle's hand-written adjoint (multi-threaded) on a bounded sample of the workload."""
     O, m, p, w = _cpu_case()
     threads = threads or os.cpu_count() or 1

@@ -187,10 +187,9 @@ __global__ void __launch_bounds__(RB, (PROD == PROD_UOC && RNGK == RNG_SOBOL) ? 
     };
 
     // ---------------------------------------------------------------------------------
-    // One unit: forward, payoff sums, adjoint seeds.  Returns the seeds in ax/aAl and
-    // whether each path is live (nonzero seed).
+    // One unit: forward, payoff sums, adjoint seeds.  The seeds of live paths (nonzero seed)
+    // go to point nSteps of their slot's fields; live[] says which paths are live.
     // ---------------------------------------------------------------------------------
-    float axOut[NP], alOut[NP];
     bool live[NP];
     auto forward = [&](int nAct, auto&& gen) {
         float x[NP], alive[NP], euro[NP], sT[NP], bLast[NP];
@@ -205,7 +204,6 @@ __global__ void __launch_bounds__(RB, (PROD == PROD_UOC && RNGK == RNG_SOBOL) ? 
             dead[a] = false;
             flag[a] = 0;
             live[a] = false;
-            axOut[a] = alOut[a] = 0.0f;
         }
         if (!nAct) return;
 
@@ -316,8 +314,6 @@ __global__ void __launch_bounds__(RB, (PROD == PROD_UOC && RNGK == RNG_SOBOL) ? 
             }
             fix_add(&paySlab[2 * (2 * nPay)], agg);
             fix_add(&paySlab[2 * (2 * nPay + 1)], agg * agg);
-            axOut[a] = ax;
-            alOut[a] = aAl;
             live[a] = ax != 0.0f || aAl != 0.0f;
             if (live[a])
             {

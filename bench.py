@@ -22,6 +22,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -359,6 +360,23 @@ def run_reference(args):
     return 0
 
 
+def run_case(args):
+    """One secondary workload alone, for profiler captures: `--case multi` is AADriskMulti of the
+    superbucket portfolio (200 Europeans, 36 monthly steps, Sobol) on a synthetic Dupire grid;
+    `--case autocall|basket` is AADriskOne of the four-asset autocall or basket (Sobol)."""
+    paths = args.paths if args.paths != NPATH else 1 << 20
+    if args.case == "multi":
+        g = tuple(int(x) for x in args.grid.split("x"))
+        sec = W.run_multi(g, paths, args.reps, args.precision)
+        print(f"AADriskMulti {g[0]}x{g[1]} {args.precision} {paths} paths: {1e3 * sec:.3f} ms per call, "
+              f"{paths / sec:.4g} paths/s")
+    else:
+        sec = W.run_md(args.case, paths, args.reps, args.precision)
+        print(f"AADriskOne 4-asset {args.case} {args.precision} {paths} paths: {1e3 * sec:.3f} ms per call, "
+              f"{paths / sec:.4g} paths/s")
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -371,10 +389,18 @@ def main():
     ap.add_argument("--serve-requests", type=int, default=10000)
     ap.add_argument("--paths", type=int, default=NPATH,
                     help="paths per step (default 2^22; smaller cases are for profiler captures only)")
+    ap.add_argument("--case", choices=["multi", "autocall", "basket"],
+                    help="time one secondary workload alone (for profiler captures) and exit: the superbucket "
+                         "portfolio's AADriskMulti, or AADriskOne of the four-asset autocall or basket")
+    ap.add_argument("--grid", default="60x30", help="--case multi: local-vol grid")
+    ap.add_argument("--reps", type=int, default=1, help="--case: timed calls after one warm-up call")
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"], help="--case: path precision")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         return run_reference(args)
+    if args.case:
+        return run_case(args)
 
     import torch
     from compfinance_gb300 import Engine, NumericalParam
@@ -435,10 +461,10 @@ def main():
             tot = float(tt.item())
         return tot, ms, launches, wall
 
-    os.makedirs(os.path.join(ROOT, "gpurun_out"), exist_ok=True)
-    with Clocks(os.path.join(ROOT, "gpurun_out", f"bench_clocks_r{rank}.csv")) as ck:
-        t32, ms32, launches, wall32 = timed(num32, args.steps, args.warmup)
-    clocks = ck.summary()
+    with tempfile.TemporaryDirectory() as tmp:
+        with Clocks(os.path.join(tmp, f"clocks_r{rank}.csv")) as ck:
+            t32, ms32, launches, wall32 = timed(num32, args.steps, args.warmup)
+        clocks = ck.summary()
     sharded = None
     if world > 1:
         from compfinance_gb300.shard import combine

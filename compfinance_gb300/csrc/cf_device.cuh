@@ -1,6 +1,6 @@
 // Device building blocks of the Monte Carlo kernels: fixed-point accumulation, the
 // mrg32k3a recurrence and its jump-ahead in integer arithmetic, Sobol points, the
-// Beasley-Springer-Moro inverse normal, and a bounded-wait bulk copy into shared memory.
+// Beasley-Springer-Moro inverse normal, and bounded-wait bulk copies into shared memory.
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -285,39 +285,68 @@ __device__ __forceinline__ unsigned sobol_state(const unsigned* dir, int stride,
 }
 
 // ---------------------------------------------------------------------------------------
-// Bulk copy global -> shared through the TMA unit (cp.async.bulk, no tensor map), completion
-// tracked by an mbarrier.  Every wait is bounded: on time-out the block records
-// DEVERR_TMA_TIMEOUT and the caller falls back to global loads.
+// Bulk copies global -> shared through the TMA unit (cp.async.bulk, no tensor map), with
+// completion tracked by an mbarrier.  Every wait is bounded.  A wait that expires records
+// DEVERR_TMA_TIMEOUT; the block then waits once more (bounded) for its copies in flight and
+// returns, so the launch fails (CF_E_DEVICE on the host) and no block computes on, or exits
+// with, a copy outstanding against its shared memory that it could still wait for.
 // Requirements: dst, src 16-byte aligned; bytes a multiple of 16 and < 2^20.
 // ---------------------------------------------------------------------------------------
-__device__ __forceinline__ bool bulk_copy_to_smem(void* dst, const void* src, unsigned bytes,
-                                                  unsigned long long* mbar, int* err)
+constexpr int MBAR_WAIT_LIMIT = 1 << 20;  // try_wait polls before a wait gives up
+
+__device__ __forceinline__ void mbar_init(unsigned long long* mbar, unsigned count)
+{
+    const unsigned bar = (unsigned)__cvta_generic_to_shared(mbar);
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// One thread: arrive on mbar expecting `bytes`, and start the copy that completes them.
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned bytes, unsigned long long* mbar)
 {
     const unsigned bar = (unsigned)__cvta_generic_to_shared(mbar);
     const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(d),
+                 "l"(src), "r"(bytes), "r"(bar)
+                 : "memory");
+}
+
+// Waits (bounded) for phase `parity` of mbar to complete; true when it did.
+__device__ __forceinline__ bool mbar_wait(unsigned long long* mbar, unsigned parity)
+{
+    const unsigned bar = (unsigned)__cvta_generic_to_shared(mbar);
+    unsigned done = 0;
+    for (int it = 0; it < MBAR_WAIT_LIMIT && !done; ++it)
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+            : "=r"(done)
+            : "r"(bar), "r"(parity)
+            : "memory");
+    return done != 0;
+}
+
+// Whole block: copies `bytes` from src into dst and waits for them.  Returns false (uniformly
+// over the block) when the wait expired; the error flag is then set and the caller must return
+// at once, without reading dst.
+__device__ __forceinline__ bool bulk_copy_to_smem(void* dst, const void* src, unsigned bytes,
+                                                  unsigned long long* mbar, int* err)
+{
     if (threadIdx.x == 0)
     {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-        asm volatile(
-            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(d),
-            "l"(src), "r"(bytes), "r"(bar)
-            : "memory");
+        mbar_init(mbar, 1);
+        bulk_load(dst, src, bytes, mbar);
     }
     __syncthreads();
-    unsigned done = 0;
-    for (int it = 0; it < (1 << 20) && !done; ++it)
-    {
-        asm volatile(
-            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n selp.u32 %0, 1, 0, p;\n}"
-            : "=r"(done)
-            : "r"(bar)
-            : "memory");
-    }
+    const bool done = mbar_wait(mbar, 0);
     const int ok = __syncthreads_and((int)done);
-    if (!ok && threadIdx.x == 0) atomicOr(err, DEVERR_TMA_TIMEOUT);
+    if (!ok)
+    {
+        if (threadIdx.x == 0) atomicOr(err, DEVERR_TMA_TIMEOUT);
+        mbar_wait(mbar, 0);  // let the copy land before the block returns (bounded)
+        __syncthreads();
+    }
     return ok != 0;
 }
 

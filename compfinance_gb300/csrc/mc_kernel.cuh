@@ -117,8 +117,10 @@ __global__ void __launch_bounds__(MC_BLOCK) mc_kernel(const McParams p)
         {
             Real* sY = reinterpret_cast<Real*>(smem + L.Y);
             const unsigned bytes = (unsigned)align16(size_t(nSteps) * nS * sizeof(Real));
-            if (bulk_copy_to_smem(sY, Y, bytes, reinterpret_cast<unsigned long long*>(smem + L.mbar), p.err))
-                Y = sY;
+            // a copy that did not complete fails the launch (error flag): the block returns
+            if (!bulk_copy_to_smem(sY, Y, bytes, reinterpret_cast<unsigned long long*>(smem + L.mbar), p.err))
+                return;
+            Y = sY;
         }
     }
     __syncthreads();

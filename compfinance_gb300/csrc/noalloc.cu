@@ -14,7 +14,10 @@
 //    cf_shapes): lowering allocates, this entry point does not.
 //  * The first call on a device looks up the array's device address (cudaGetSymbolAddress,
 //    once per device, with that device current); make that first call before any stream
-//    capture.
+//    capture.  The address is kept for the life of the process, which assumes the device's
+//    primary context lives as long: after a cudaDeviceReset the library must be reloaded.
+//  * Black-Scholes and Dupire models only; a multi-asset plan is refused (CF_E_UNSUPPORTED)
+//    before anything is launched.
 //  * Every call shares the array: calls that overlap on the GPU (other threads, other
 //    streams) race.  Each call clears what must start at zero (accumulators, error flag).
 //  * Requests whose scratch cannot fit even one block per launch, or whose accumulators
@@ -109,6 +112,10 @@ extern "C" int cf_aad_risk_aggregate_noalloc(cf_context* ctx, const char* modelI
     for (auto& kv : c.plans)
         if (kv.first.first == modelId && kv.first.second == productId) plan = kv.second.get();
     if (!plan) return fail_c(CF_E_NOTFOUND, "noalloc: (model, product) not lowered yet; call cf_shapes first");
+    // the multi-asset model runs its own kernels (md_kernel.cu) with derived-quantity
+    // accumulators; only the single-asset Black-Scholes and Dupire kernels run here
+    if (plan->model != MODEL_BS && plan->model != MODEL_DUPIRE)
+        return fail_c(CF_E_UNSUPPORTED, "noalloc: only Black-Scholes and Dupire models are supported");
     {
         auto mi = c.models.find(modelId);
         auto pi = c.products.find(productId);

@@ -168,8 +168,7 @@ def serving_stream(n=10000, rate=2000.0, seed=2026):
 
 # ---------------------------------------------------------------------------------------
 # Portfolio risk run (AADriskMulti of the superbucket portfolio on a synthetic Dupire surface)
-# for timing and profiling:
-#     python -m compfinance_gb300.workloads multi [GRID=60x30] [PATHS=1048576] [REPS=1] [fp32|fp64]
+# for timing and profiling (bench.py --case multi)
 # ---------------------------------------------------------------------------------------
 def run_multi(grid=(60, 30), paths=1 << 20, reps=1, precision="fp32", device=0):
     """Times `reps` AADriskMulti calls (200 payoffs x (1 + nS nT) parameters, 36 monthly steps,
@@ -236,23 +235,3 @@ def run_md(product="autocall", paths=1 << 20, reps=1, precision="fp32", risk=Tru
     eng.close()
     return dt
 
-
-if __name__ == "__main__":
-    import sys
-    a = sys.argv[1:]
-    if a and a[0] in ("autocall", "basket"):
-        n = int(a[1]) if len(a) > 1 else 1 << 20
-        r = int(a[2]) if len(a) > 2 else 1
-        prec = a[3] if len(a) > 3 else "fp32"
-        sec = run_md(a[0], n, r, prec)
-        print(f"AADriskOne 4-asset {a[0]} {prec} {n} paths: {1e3 * sec:.3f} ms per call, {n / sec:.4g} paths/s")
-        raise SystemExit(0)
-    if not a or a[0] != "multi":
-        raise SystemExit("usage: python -m compfinance_gb300.workloads multi [GRID] [PATHS] [REPS] [fp32|fp64]\n"
-                         "       python -m compfinance_gb300.workloads autocall|basket [PATHS] [REPS] [fp32|fp64]")
-    g = tuple(int(x) for x in (a[1] if len(a) > 1 else "60x30").split("x"))
-    n = int(a[2]) if len(a) > 2 else 1 << 20
-    r = int(a[3]) if len(a) > 3 else 1
-    prec = a[4] if len(a) > 4 else "fp32"
-    sec = run_multi(g, n, r, prec)
-    print(f"AADriskMulti {g[0]}x{g[1]} {prec} {n} paths: {1e3 * sec:.3f} ms per call, {n / sec:.4g} paths/s")

@@ -22,7 +22,7 @@ driver ``oracle/ref_driver.cpp`` (which includes ``main.h`` once).  Flags:
 ``-std=c++17 -O2 -ffp-contract=off``; no ``-ffast-math`` (the reference's own
 project uses ``/fp:fast``; the oracle must not).
 
-Usage: ``python3 oracle/build_ref.py [--reference DIR]``.  Exit status 0 and the
+Usage: ``python3 oracle/build_ref.py --reference DIR`` (or ``CF_REFERENCE_DIR=DIR``).  Exit status 0 and the
 binary path on stdout on success; exit status 2 when the reference is absent.
 """
 import argparse
@@ -118,5 +118,9 @@ def build(reference):
 
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default=os.environ.get("CF_REFERENCE_DIR", "/root/reference"))
-    sys.exit(build(ap.parse_args().reference))
+    ap.add_argument("--reference", default=os.environ.get("CF_REFERENCE_DIR"),
+                    help="the reference checkout (or CF_REFERENCE_DIR); required")
+    a = ap.parse_args()
+    if not a.reference:
+        ap.error("the reference checkout is required: --reference DIR or CF_REFERENCE_DIR")
+    sys.exit(build(a.reference))

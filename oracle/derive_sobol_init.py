@@ -4,10 +4,11 @@ of each Sobol dimension from the expanded direction-number table of the referenc
 (sobol.cpp: 32 direction numbers x 1111 dimensions, Joe & Kuo's "old" 1111-dimension set).
 
 The library regenerates the full table from this compact data with the Joe-Kuo
-recurrence (compfinance_gb300/csrc/sobol_dirs.cpp), so the points are bit-identical
-without carrying the expanded table.  Usage:
+recurrence (compfinance_gb300/csrc/host_math.cpp), so the points are bit-identical
+without carrying the expanded table.  An offline recipe: it reads the reference's
+sobol.cpp, whose path is a required argument.  Usage:
 
-    python3 compfinance_gb300/data/derive_sobol_init.py [sobol.cpp] > compfinance_gb300/data/sobol_joe_kuo.inc
+    python3 oracle/derive_sobol_init.py REFERENCE_DIR/sobol.cpp > compfinance_gb300/data/sobol_joe_kuo.inc
 
 The output is a C/C++ initializer list included by the library and by the oracle.
 """
@@ -46,12 +47,14 @@ def derive(col):
 
 
 def main():
-    path = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/sobol.cpp"
+    if len(sys.argv) != 2:
+        raise SystemExit("usage: python3 oracle/derive_sobol_init.py REFERENCE_DIR/sobol.cpp")
+    path = sys.argv[1]
     dirs = parse(path)
     ndim = len(dirs[0])
     print("/* Joe-Kuo Sobol initialisation data ('old' set), %d dimensions." % ndim)
     print(" * One entry per dimension: {s, a, {m_1, ..., m_s}}; dimension 0 is van der Corput (s=0).")
-    print(" * Generated by compfinance_gb300/data/derive_sobol_init.py. */")
+    print(" * Generated by oracle/derive_sobol_init.py. */")
     print("#define CF_SOBOL_MAX_DIM %d" % ndim)
     for d in range(ndim):
         col = [dirs[i][d] for i in range(32)]

@@ -9,6 +9,7 @@ the tests never need the reference.
 
     python3 tests/golden/make_golden.py [rng host mc calib bump products multi_asset]   # all when none named;
                                                                    # rebuilds the driver when missing
+                                                                   # (from CF_REFERENCE_DIR)
 """
 import json
 import os
@@ -28,7 +29,10 @@ M1P1 = 4294967088.0
 
 def run(cmds):
     if not os.path.exists(DRIVER):
-        subprocess.check_call([sys.executable, os.path.join(ROOT, "oracle", "build_ref.py")])
+        ref = os.environ.get("CF_REFERENCE_DIR")
+        if not ref:
+            raise SystemExit("oracle/_ref/ref_driver is missing: set CF_REFERENCE_DIR to the reference checkout")
+        subprocess.check_call([sys.executable, os.path.join(ROOT, "oracle", "build_ref.py"), "--reference", ref])
     out = subprocess.run([DRIVER], input="\n".join(cmds) + "\n", capture_output=True, text=True,
                          check=True).stdout
     res = []

@@ -177,6 +177,12 @@ struct McParams
     int nodeShiftF;
     long long nodeSlabOffset;
     const float* invnF;   // [512][4] piecewise-cubic inverse normal of the launch's generator
+    // dupire_risk32: per step (colA, colB, time weights A and B in units of 2^-nodeShiftF as
+    // float bits), the node columns and weights of the reverse sweep's local-vol adjoints
+    const int4* stepcF;
+    // dupire_risk32: local-vol rows staged into shared memory by bulk copies, rowChunk steps per
+    // copy, double-buffered (0: rows are read through L1)
+    int rowChunk;
 
     // multi-asset displaced model (mcMdlMultiDisplaced.h) with Baskets / Autocall
     // (mcPrdMulti.h); nSteps is the number of time steps, the Gaussians per path nSteps * nA
@@ -203,12 +209,16 @@ struct McLaunch
     int model, prod, rng, fp32, risk;
     int grid, block;
     size_t smem;
-    int fast;             // 1: FP32 Dupire risk through dupire_risk32
+    int fast;             // FP32 Dupire risk through dupire_risk32: 1 (rows read through L1) or 2
+                          // (rows staged by bulk copies, p.rowChunk > 0)
 };
 
 int launch_mc(const McLaunch& l, const McParams& p, void* stream);   // returns cudaError_t
 int mc_smem_bytes(const McLaunch& l, const McParams& p, int stageY, size_t* bytes);
 int mc_occupancy(const McLaunch& l, size_t smem, int* blocksPerSM);
+// dupire_risk32 staging (p.stageY: inverse-normal table in shared memory; p.rowChunk: local-vol
+// rows staged by bulk copies) that keeps occ0 blocks per SM; sets *smem, returns the occupancy.
+int r32_staging(McLaunch& l, McParams& p, int occ0, size_t* smem);
 // dupire_risk32 keeps the reverse-sweep scratch of its last R32_RING unit rounds (a live path
 // may wait up to two rounds before its sweep); round r uses slot r mod R32_RING, so a launch
 // of fewer rounds needs only as many slots as it has rounds.

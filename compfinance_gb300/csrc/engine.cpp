@@ -368,7 +368,7 @@ int Context::buildPlan(const ModelDesc& m, const ProductDesc& pd, Plan& plan)
     std::vector<double> ev(10 * size_t(plan.nEv), 0.0);
     double frontSpot = m.spot;
     size_t oBs = 0, oX = 0, oInv = 0, oY = 0, oXf = 0, oInvf = 0, oYf = 0, oCA = 0, oCB = 0, oCAf = 0, oCBf = 0,
-           oColA = 0, oColB = 0, oBsF = 0, oBucket = 0, oWA = 0, oWB = 0, oXs = 0, oIr = 0, oTd = 0, oBf = 0, oVols = 0, oSq = 0, oTw = 0;
+           oColA = 0, oColB = 0, oBsF = 0, oBucket = 0, oWA = 0, oWB = 0, oXs = 0, oIr = 0, oTd = 0, oBf = 0, oVols = 0, oSq = 0, oTw = 0, oSc = 0;
 
     if (m.kind == MODEL_BS)
     {
@@ -548,6 +548,18 @@ int Context::buildPlan(const ModelDesc& m, const ProductDesc& pd, Plan& plan)
             const double perWord = 256.0 * sMax * 512.0 * std::max(wMax, 1e-300);
             const int shift = int(std::floor(std::log2(1073741824.0 / perWord)));  // one bit of margin
             P.nodeShiftF = std::min(FIX_HI_SHIFT, shift);
+            // the reverse sweep's per-step node columns and weights (float, scaled by 2^nodeShiftF,
+            // exact: a power of two)
+            std::vector<int> scv(4 * size_t(n));
+            for (int i = 0; i < n; ++i)
+            {
+                const float wa = std::ldexp(float(cAv[i]), P.nodeShiftF), wb = std::ldexp(float(cBv[i]), P.nodeShiftF);
+                scv[4 * size_t(i)] = colA[i];
+                scv[4 * size_t(i) + 1] = colB[i];
+                std::memcpy(&scv[4 * size_t(i) + 2], &wa, 4);
+                std::memcpy(&scv[4 * size_t(i) + 3], &wb, 4);
+            }
+            oSc = pk.vec(scv);
             P.fast32 = (pd.kind == PROD_UOC || pd.kind == PROD_EUROPEAN) && evOk && nS <= 510 && bg.ok &&
                        bg.oneCompare && shift >= 4;
             // FP32 AADriskMulti (multi_risk32.cu) uses the same tables and slab unit: its chunks
@@ -635,6 +647,7 @@ int Context::buildPlan(const ModelDesc& m, const ProductDesc& pd, Plan& plan)
         P.xsF = (const float*)D(oXs);
         P.irF = (const float*)D(oIr);
         P.tdF = (const float*)D(oTd);
+        P.stepcF = (const int4*)D(oSc);
         P.bucketF = (const int*)D(oBf);
         P.volsD = (const double*)D(oVols);
         P.stepSqD = (const double*)D(oSq);
@@ -780,17 +793,13 @@ int Context::enqueue(Slot& slot, Plan& plan, const cf_num_param& num, bool risk,
     l.fast = mc_use_fast32(plan.base, plan.prod, l.fp32, l.risk);
     if (l.fast)
     {
-        // the inverse-normal table goes to shared memory when that costs no occupancy
+        // the local-vol rows (bulk copies) and the inverse-normal table go to shared memory when
+        // that costs no occupancy
         p.stageY = 0;
+        p.rowChunk = 0;
         mc_smem_bytes(l, p, 0, &smem0);
         if (smem0 > 200 * 1024 || mc_occupancy(l, smem0, &occ0) || occ0 < 1) l.fast = 0;
-        else
-        {
-            p.stageY = 1;
-            mc_smem_bytes(l, p, 1, &smem1);
-            if (mc_occupancy(l, smem1, &occ1) || occ1 < occ0) p.stageY = 0;
-            else smem0 = smem1;
-        }
+        else occ0 = r32_staging(l, p, occ0, &smem0);
     }
     if (!l.fast)
     {

@@ -28,6 +28,11 @@
 //     added to the accumulators once, at the end.  Each contribution is rounded once, so
 //     every sum is independent of how paths are grouped into warps, blocks, chunks and
 //     launches.
+//
+// The kernel template is instantiated in two translation units: mc_dupire_risk32_l1.cu (the
+// forward reads the local-vol rows through L1) and mc_dupire_risk32_tma.cu (rows staged into
+// shared memory by bulk copies), so that each kernel holds one form of the forward.
+#pragma once
 #include <cuda_runtime.h>
 
 #include "cf_device.cuh"
@@ -58,7 +63,7 @@ __host__ __device__ inline size_t a16(size_t x) { return (x + 15) & ~size_t(15);
 
 struct R32Layout
 {
-    size_t slab, node, xs, ir, bucket, listIdx, cnt, stepc, invn, base, total;
+    size_t slab, node, xs, ir, bucket, listIdx, cnt, mbar, stepc, invn, rows, base, total;
 };
 
 __host__ __device__ inline R32Layout r32_layout(int rng, const McParams& p)
@@ -79,10 +84,14 @@ __host__ __device__ inline R32Layout r32_layout(int rng, const McParams& p)
     off += a16(size_t(LIST_CAP) * 2);
     L.cnt = off;
     off += 16;
-    L.stepc = off;  // (colA, colB, weight A, weight B in units of 2^-nodeShiftF) per step
+    L.mbar = off;   // completion barriers of the two row buffers
+    off += 16;
+    L.stepc = off;  // per-step node columns and weights of the reverse
     off += a16(size_t(p.nSteps) * 16);
     L.invn = off;   // piecewise-cubic inverse normal, 512 pieces (when staged: p.stageY)
     if (p.stageY) off += size_t(512) * 16;
+    L.rows = off;   // two buffers of rowChunk local-vol rows (y - 2d, d)[nS + 1]
+    if (p.rowChunk) off += a16(size_t(2) * p.rowChunk * (p.nS + 1) * 8);
     L.base = off;
     if (rng == RNG_SOBOL) off += a16(size_t(RW) * (size_t(p.nSteps) | 1) * 4);
     L.total = off;
@@ -92,7 +101,7 @@ __host__ __device__ inline R32Layout r32_layout(int rng, const McParams& p)
 // Nine blocks per SM (56 registers) where that costs no spills: the kernel is bound by issue
 // and latency, and a ninth block hides more of it (60x30 barrier, mrg32k3a: 3.8% faster).  The
 // Sobol barrier variant would spill at 56 registers and keeps eight.
-template <int PROD, int RNGK>
+template <int PROD, int RNGK, bool ROWS>
 __global__ void __launch_bounds__(RB, (PROD == PROD_UOC && RNGK == RNG_SOBOL) ? 8 : 9)
     dupire_risk32(const McParams p)
 {
@@ -108,8 +117,10 @@ __global__ void __launch_bounds__(RB, (PROD == PROD_UOC && RNGK == RNG_SOBOL) ? 
     int* sBucket = reinterpret_cast<int*>(smem + L.bucket);
     unsigned short* listIdx = reinterpret_cast<unsigned short*>(smem + L.listIdx);
     int* cnt = reinterpret_cast<int*>(smem + L.cnt);
-    int4* stepc = reinterpret_cast<int4*>(smem + L.stepc);
+    unsigned long long* mbar = reinterpret_cast<unsigned long long*>(smem + L.mbar);
+    int4* sStepc = reinterpret_cast<int4*>(smem + L.stepc);
     float4* sInvn = reinterpret_cast<float4*>(smem + L.invn);
+    float2* sRows = reinterpret_cast<float2*>(smem + L.rows);
 
     const int tid = threadIdx.x, lane = tid & 31, wib = tid >> 5;
     const int nS = p.nS, nT = p.nT, nSteps = p.nSteps, nPay = p.nPay, nNodes = nS * nT;
@@ -118,7 +129,12 @@ __global__ void __launch_bounds__(RB, (PROD == PROD_UOC && RNGK == RNG_SOBOL) ? 
     // written only by thread i mod RB
     long long* gnode = reinterpret_cast<long long*>(static_cast<char*>(p.scratch) + p.nodeSlabOffset) +
                        size_t(blockIdx.x) * nNodes;
-    const float wScale = ldexpf(1.0f, p.nodeShiftF);
+    const int K = ROWS ? p.rowChunk : 0;  // the host launches ROWS kernels with an even rowChunk >= 2
+    if (ROWS && tid == 0)
+    {
+        mbar_init(mbar, 1);
+        mbar_init(mbar + 1, 1);
+    }
     for (int i = tid; i < 2 * (4 + 2 * nPay + 2); i += RB) slab[i] = 0;
     for (int i = tid; i < nNodes; i += RB)
     {
@@ -132,8 +148,7 @@ __global__ void __launch_bounds__(RB, (PROD == PROD_UOC && RNGK == RNG_SOBOL) ? 
     const bool stageInvn = p.stageY != 0;
     if (stageInvn)
         for (int i = tid; i < 512; i += RB) sInvn[i] = gInvn[i];
-    for (int i = tid; i < nSteps; i += RB)
-        stepc[i] = make_int4(p.colA[i], p.colB[i], __float_as_int(p.cAf[i] * wScale), __float_as_int(p.cBf[i] * wScale));
+    for (int i = tid; i < nSteps; i += RB) sStepc[i] = p.stepcF[i];
     __syncthreads();
 
     const float2* td = reinterpret_cast<const float2*>(p.tdF);
@@ -190,8 +205,21 @@ __global__ void __launch_bounds__(RB, (PROD == PROD_UOC && RNGK == RNG_SOBOL) ? 
     // One unit: forward, payoff sums, adjoint seeds.  The seeds of live paths (nonzero seed)
     // go to point nSteps of their slot's fields; live[] says which paths are live.
     // ---------------------------------------------------------------------------------
+    // Local-vol rows of the forward: with K = rowChunk > 0, chunk c (steps [cK, cK + K)) is
+    // copied into row buffer c mod 2 by one bulk copy, issued when chunk c - 1 starts, so it
+    // has landed by the time chunk c needs it; otherwise rows are read through L1.
+    unsigned rowPhase = 0;  // bit b: parity of the next completion of buffer b (uniform)
+    auto issueRows = [&](int c) {  // thread 0
+        const int s0 = c * K, n = min(K, nSteps - s0);
+        // rows start on 16-byte boundaries (K is even, a row is 8 (nS + 1) bytes); the size is
+        // rounded up to 16 bytes inside the table's 16-byte padded region
+        bulk_load(sRows + (c & 1) * K * tPitch, td + size_t(s0) * tPitch, unsigned(a16(size_t(n) * tPitch * 8)),
+                  mbar + (c & 1));
+    };
+
     bool live[NP];
-    auto forward = [&](int nAct, auto&& gen) {
+    // Returns false (uniformly) when a row copy did not complete: the block must then return.
+    auto forward = [&](int nAct, auto&& gen) -> bool {
         float x[NP], alive[NP], euro[NP], sT[NP], bLast[NP];
         bool dead[NP];
         unsigned flag[NP];
@@ -205,7 +233,6 @@ __global__ void __launch_bounds__(RB, (PROD == PROD_UOC && RNGK == RNG_SOBOL) ? 
             flag[a] = 0;
             live[a] = false;
         }
-        if (!nAct) return;
 
         // product date at point i (i < nSteps: monitoring only; i == nSteps: maturity)
         auto event = [&](int i, int a) {
@@ -245,40 +272,73 @@ __global__ void __launch_bounds__(RB, (PROD == PROD_UOC && RNGK == RNG_SOBOL) ? 
             }
         };
 
-        if (p.evAtStep[0] >= 0)
+        if (nAct && p.evAtStep[0] >= 0)
 #pragma unroll
             for (int a = 0; a < NP; ++a)
                 if (a < nAct) event(0, a);
-        for (int s = 0; s < nSteps; ++s)
-        {
-            const float g = gen(s);
-            __stcs(fs + F_G * rowStride + s * Ti + myCol, g);  // streamed: read once, in the reverse
-            const float2* trow = td + size_t(s) * tPitch;
-#pragma unroll
-            for (int a = 0; a < NP; ++a)
+        // steps [s0, s1), with the local-vol entry of interval lo at step s given by row(s, lo)
+        auto steps = [&](int s0, int s1, auto&& row) {
+            for (int s = s0; s < s1; ++s)
             {
-                if (a >= nAct) break;
-                const float ga = a ? -g : g;
-                const int lo = search(x[a]);
-                const float2 ir = sIr[lo];
-                const float t2 = fminf((x[a] - ir.x) * ir.y, T_MAX) + 2.0f;
-                const unsigned tq = __float_as_uint(t2) & T_MASK;
-                const float2 yd = __ldg(trow + lo);
-                const float v = fmaf(yd.y, t2, yd.x);  // table (y - 2 d, d)
-                __stcs(reinterpret_cast<unsigned*>(fs) + (F_W + a) * rowStride + s * Ti + myCol,
-                       (unsigned(lo) << LO_SHIFT) | flag[a] | tq);
-                flag[a] = 0;  // the flag of point s + 1 is set by its date, if any
-                x[a] += v * (-0.5f * v + ga);
-            }
-            // the barrier monitors at dates only (and a date below the band needs nothing before
-            // maturity: one test for both paths of the pair); a European's one date is the last point
-            if (UOC ? (evEvery || __ldg(p.evAtStep + s + 1) >= 0) &&
-                          (s + 1 == nSteps || fmaxf(x[0], x[NP - 1]) > logBand)
-                    : s + 1 == nSteps)
+                const float g = gen(s);
+                __stcs(fs + F_G * rowStride + s * Ti + myCol, g);  // streamed: read once, in the reverse
 #pragma unroll
                 for (int a = 0; a < NP; ++a)
-                    if (a < nAct) event(s + 1, a);
+                {
+                    if (a >= nAct) break;
+                    const float ga = a ? -g : g;
+                    const int lo = search(x[a]);
+                    const float2 ir = sIr[lo];
+                    const float t2 = fminf((x[a] - ir.x) * ir.y, T_MAX) + 2.0f;
+                    const unsigned tq = __float_as_uint(t2) & T_MASK;
+                    const float2 yd = row(s, lo);
+                    const float v = fmaf(yd.y, t2, yd.x);  // table (y - 2 d, d)
+                    __stcs(reinterpret_cast<unsigned*>(fs) + (F_W + a) * rowStride + s * Ti + myCol,
+                           (unsigned(lo) << LO_SHIFT) | flag[a] | tq);
+                    flag[a] = 0;  // the flag of point s + 1 is set by its date, if any
+                    x[a] += v * (-0.5f * v + ga);
+                }
+                // the barrier monitors at dates only (and a date below the band needs nothing
+                // before maturity: one test for both paths of the pair); a European's one date
+                // is the last point
+                if (UOC ? (evEvery || __ldg(p.evAtStep + s + 1) >= 0) &&
+                              (s + 1 == nSteps || fmaxf(x[0], x[NP - 1]) > logBand)
+                        : s + 1 == nSteps)
+#pragma unroll
+                    for (int a = 0; a < NP; ++a)
+                        if (a < nAct) event(s + 1, a);
+            }
+        };
+        if constexpr (ROWS)
+        {
+            // every thread of the block takes part in the chunk loop (its barriers), with or
+            // without a unit; a buffer is rewritten only after all threads passed the barrier
+            // of the chunk that follows the one that read it
+            const int nChunks = (nSteps + K - 1) / K;
+            if (tid == 0) issueRows(0);  // buffer 0 was last read before the previous round's list barrier
+            for (int c = 0; c < nChunks; ++c)
+            {
+                const int b = c & 1;
+                const bool done = mbar_wait(mbar + b, (rowPhase >> b) & 1u);
+                rowPhase ^= 1u << b;
+                if (!__syncthreads_and(done))
+                {
+                    if (tid == 0) atomicOr(p.err, DEVERR_TMA_TIMEOUT);
+                    mbar_wait(mbar + b, ((rowPhase >> b) & 1u) ^ 1u);  // let the late copy land (bounded)
+                    __syncthreads();
+                    return false;
+                }
+                if (tid == 0 && c + 1 < nChunks) issueRows(c + 1);
+                const float2* buf = sRows + b * K * tPitch;  // row s at buf + (s - cK) tPitch
+                const int s0 = c * K;
+                if (nAct) steps(s0, min(s0 + K, nSteps), [&](int s, int lo) { return buf[(s - s0) * tPitch + lo]; });
+            }
         }
+        else
+        {
+            if (nAct) steps(0, nSteps, [&](int s, int lo) { return __ldg(td + size_t(s) * tPitch + lo); });
+        }
+        if (!nAct) return true;
 
         // payoffs, sums, adjoint seeds
 #pragma unroll
@@ -321,6 +381,7 @@ __global__ void __launch_bounds__(RB, (PROD == PROD_UOC && RNGK == RNG_SOBOL) ? 
                 if (UOC) fs[(F_B + a) * rowStride + seedRow + myCol] = aAl;
             }
         }
+        return true;
     };
 
     // contribution c (units of 1) to spot j of a step's vol row (its columns and weights in
@@ -438,7 +499,7 @@ __global__ void __launch_bounds__(RB, (PROD == PROD_UOC && RNGK == RNG_SOBOL) ? 
                     const int jl = lo - (lo > 0 ? 1 : 0);
                     const bool inner = lo > 0 && lo < nS;  // two spot knots; one at the flat ends
                     const float cR = av * t, cL = av - cR;
-                    const int4 sc = stepc[s];
+                    const int4 sc = sStepc[s];
                     if (fabsf(av) < AV_MAX)
                     {
                         const float wa = __int_as_float(sc.z), wb = __int_as_float(sc.w);
@@ -522,11 +583,12 @@ __global__ void __launch_bounds__(RB, (PROD == PROD_UOC && RNGK == RNG_SOBOL) ? 
             const long long u = u0 + it;
             const int nAct = u < u1 ? ((2 * u + 1 < p.nPath) ? 2 : 1) : 0;
             const int slot = slotOf(it);
-            forward(nAct, [&](int) {
-                const unsigned d = mrg_next(st);   // in [1, m1]; uniform d / (m1 + 1)
-                const bool sup = d > 2147483544u;  // (m1 + 1) / 2
-                return gaussT(sup ? 4294967088u - d : d, sup);
-            });
+            if (!forward(nAct, [&](int) {
+                    const unsigned d = mrg_next(st);   // in [1, m1]; uniform d / (m1 + 1)
+                    const bool sup = d > 2147483544u;  // (m1 + 1) / 2
+                    return gaussT(sup ? 4294967088u - d : d, sup);
+                }))
+                return;  // a row copy failed (error flag set): the launch fails
             endRound(slot);
         }
     }
@@ -553,11 +615,12 @@ __global__ void __launch_bounds__(RB, (PROD == PROD_UOC && RNGK == RNG_SOBOL) ? 
                 nAct = (n >= 1 && n <= p.nPath) ? 1 : 0;
             }
             const int slot = slotOf(it);
-            forward(nAct, [&](int i) {
-                const unsigned sb = base[i] ^ sobol_state(p.sobolDir, nSteps, i, (unsigned long long)lane);
-                const bool sup = sb >= 2147483648u;
-                return gaussT(sup ? 0u - sb : (sb > 1u ? sb : 1u), sup);  // state 0 occurs only at index 0
-            });
+            if (!forward(nAct, [&](int i) {
+                    const unsigned sb = base[i] ^ sobol_state(p.sobolDir, nSteps, i, (unsigned long long)lane);
+                    const bool sup = sb >= 2147483648u;
+                    return gaussT(sup ? 0u - sb : (sb > 1u ? sb : 1u), sup);  // state 0 occurs only at index 0
+                }))
+                return;  // a row copy failed (error flag set): the launch fails
             endRound(slot);
         }
     }
@@ -577,15 +640,14 @@ __global__ void __launch_bounds__(RB, (PROD == PROD_UOC && RNGK == RNG_SOBOL) ? 
 
 }  // namespace
 
-const void* dupire_risk32_ptr(int prod, int rng)
+template <bool ROWS>
+const void* dupire_risk32_ptr_t(int prod, int rng)
 {
-    if (prod == PROD_UOC && rng == RNG_MRG) return (const void*)&dupire_risk32<PROD_UOC, RNG_MRG>;
-    if (prod == PROD_UOC && rng == RNG_SOBOL) return (const void*)&dupire_risk32<PROD_UOC, RNG_SOBOL>;
-    if (prod == PROD_EUROPEAN && rng == RNG_MRG) return (const void*)&dupire_risk32<PROD_EUROPEAN, RNG_MRG>;
-    if (prod == PROD_EUROPEAN && rng == RNG_SOBOL) return (const void*)&dupire_risk32<PROD_EUROPEAN, RNG_SOBOL>;
+    if (prod == PROD_UOC && rng == RNG_MRG) return (const void*)&dupire_risk32<PROD_UOC, RNG_MRG, ROWS>;
+    if (prod == PROD_UOC && rng == RNG_SOBOL) return (const void*)&dupire_risk32<PROD_UOC, RNG_SOBOL, ROWS>;
+    if (prod == PROD_EUROPEAN && rng == RNG_MRG) return (const void*)&dupire_risk32<PROD_EUROPEAN, RNG_MRG, ROWS>;
+    if (prod == PROD_EUROPEAN && rng == RNG_SOBOL) return (const void*)&dupire_risk32<PROD_EUROPEAN, RNG_SOBOL, ROWS>;
     return nullptr;
 }
-
-size_t dupire_risk32_smem(int rng, const McParams& p) { return r32_layout(rng, p).total; }
 
 }  // namespace cf

@@ -2,6 +2,7 @@
 // the launch itself (cudaLaunchKernel on the caller's stream).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdlib>
 
 #include "mc_kernel.cuh"
@@ -12,12 +13,13 @@ const void* mc_kernel_ptr_bs_f64(int prod, int rng, int risk);
 const void* mc_kernel_ptr_bs_f32(int prod, int rng, int risk);
 const void* mc_kernel_ptr_dupire_f64(int prod, int rng, int risk);
 const void* mc_kernel_ptr_dupire_f32(int prod, int rng, int risk);
-const void* dupire_risk32_ptr(int prod, int rng);
+const void* dupire_risk32_ptr_l1(int prod, int rng);
+const void* dupire_risk32_ptr_tma(int prod, int rng);
 size_t dupire_risk32_smem(int rng, const McParams& p);
 
 static const void* kernel_ptr(const McLaunch& l)
 {
-    if (l.fast) return dupire_risk32_ptr(l.prod, l.rng);
+    if (l.fast) return l.fast == 2 ? dupire_risk32_ptr_tma(l.prod, l.rng) : dupire_risk32_ptr_l1(l.prod, l.rng);
     if (l.model == MODEL_BS)
         return l.fp32 ? mc_kernel_ptr_bs_f32(l.prod, l.rng, l.risk) : mc_kernel_ptr_bs_f64(l.prod, l.rng, l.risk);
     return l.fp32 ? mc_kernel_ptr_dupire_f32(l.prod, l.rng, l.risk)
@@ -70,6 +72,54 @@ int mc_use_fast32(const McParams& plan, int prod, int fp32, int risk)
     if (!plan.fast32 || !fp32 || !risk || (prod != PROD_UOC && prod != PROD_EUROPEAN)) return 0;
     const char* env = std::getenv("CF_FAST32");
     return env && env[0] == '0' ? 0 : 1;
+}
+
+int r32_staging(McLaunch& l, McParams& p, int occ0, size_t* smem)
+{
+    // p.stageY: the inverse-normal table in shared memory; p.rowChunk: local-vol rows per bulk
+    // copy (0: rows read through L1)
+    auto occOf = [&](int stage, int chunk, size_t* b) {
+        p.stageY = stage;
+        p.rowChunk = chunk;
+        l.fast = chunk ? 2 : 1;  // the kernel form with (2) or without (1) staged rows
+        int occ = 0;
+        mc_smem_bytes(l, p, 0, b);
+        if (*b > 200 * 1024 || mc_occupancy(l, *b, &occ)) return 0;
+        return occ;
+    };
+    int stage = 0, chunk = 0;
+    size_t b1 = 0;
+    const char* envK = std::getenv("CF_ROW_CHUNK");
+    if (envK)
+    {
+        // a forced row chunk (tests and tuning; even, at most 16), taken at whatever occupancy
+        // it leaves, with the inverse-normal table staged when that costs nothing more
+        chunk = std::max(0, std::min(16, std::atoi(envK))) & ~1;
+        const int o0 = occOf(0, chunk, &b1);
+        stage = occOf(1, chunk, &b1) >= o0 ? 1 : 0;
+    }
+    else
+    {
+        // (inverse-normal table staged, rows per bulk copy), in order of preference; the first
+        // that keeps the occupancy of the unstaged kernel is taken
+        static const int opts[][2] = {{1, 8}, {0, 8}, {1, 4}, {0, 4}, {1, 2}, {0, 2}, {1, 0}};
+        for (const auto& o : opts)
+        {
+            const int occ = occOf(o[0], o[1], &b1);
+            if (occ >= 1 && occ >= occ0)
+            {
+                stage = o[0];
+                chunk = o[1];
+                break;
+            }
+        }
+    }
+    // the chosen configuration is measured last: that also leaves the kernel's dynamic
+    // shared-memory limit at the size it launches with
+    const int occ = occOf(stage, chunk, smem);
+    if (occ >= 1) return occ;
+    occOf(0, 0, smem);
+    return occ0;
 }
 
 int mc_occupancy(const McLaunch& l, size_t smem, int* blocksPerSM)

@@ -277,6 +277,35 @@ def test_tma_staged_local_vols_bit_identical(eng, monkeypatch, precision):
     assert np.abs(out["1"]["risks"]).max() > 0
 
 
+@pytest.mark.parametrize("grid", [(20, 10), (60, 30), (120, 60)])
+def test_fp32_risk_rows_staged_bit_identical(eng, monkeypatch, grid):
+    """The FP32 risk kernel with its forward's local-vol rows staged into shared memory by bulk
+    copies (CF_ROW_CHUNK = 2, 4, 8 steps per copy, two buffers) and read through L1 (0): the same
+    numbers bit for bit, for the barrier (156 weekly steps, a multiple of every chunk, and 155,
+    whose last chunk is short) and the European, both generators, with a partial last round of
+    units; no device error flag (every bounded wait on a copy completed)."""
+    from compfinance_gb300 import workloads as W
+    s, t, v = W.dupire_surface(*grid)
+    u = W.UOC_BARRIER
+    name = f"rows{grid[0]}"
+    eng.putDupire(W.DUPIRE_SPOT, s, t, v, W.DUPIRE_MAXDT, name)
+    eng.putBarrier(u["strike"], u["barrier"], u["maturity"], u["monitor_freq"], u["smooth"], 0, "rows_uoc156")
+    T155 = 155 * u["monitor_freq"]
+    eng.putBarrier(u["strike"], u["barrier"], T155, u["monitor_freq"], u["smooth"], 0, "rows_uoc155")
+    eng.putEuropean(110.0, 3.0, 3.0, "rows_eu")
+    assert eng.shapes(name, "rows_uoc155")[2] == 155
+    for prod in ("rows_uoc156", "rows_uoc155", "rows_eu"):
+        for sob in (0, 1):
+            out = {}
+            for k in ("0", "2", "4", "8"):
+                monkeypatch.setenv("CF_ROW_CHUNK", k)
+                out[k] = eng.AADriskOne(name, prod, num(sob, (1 << 16) + 4001, "fp32"))
+            assert np.abs(out["0"]["risks"]).max() > 0
+            for k in ("2", "4", "8"):
+                assert np.array_equal(out[k]["payoffValues"], out["0"]["payoffValues"]), (prod, sob, k)
+                assert np.array_equal(out[k]["risks"], out["0"]["risks"]), (prod, sob, k)
+
+
 @pytest.mark.parametrize("prod", ["uoc", "european"])
 def test_fp32_risk_kernel_one_spot_knot(eng, prod):
     """A local vol flat in spot (one spot knot, 30 times): the FP32 risk kernel against FP64 on

@@ -370,6 +370,30 @@ class Engine:
         return dict(value=val.value, delta=dl.value, strikes=k, mats=m, vega=vega.reshape(len(k), len(m)),
                     microbucket=micro.reshape(nS.value, nT.value))
 
+    def calibAdjoint(self, ivs, inclSpots, maxDs, inclTimes, maxDtVol, strikes, mats, micro, refSeeding=False):
+        """The calibration's adjoint alone (test hook): local-vol adjoints micro[nS][nT] -> vega
+        [strike][mat] of the risk view; with, per node and point ([nT][nS][5] each), the forward's
+        call prices and their derivatives to the implied vol that it was taken at, and the adjoint
+        of each point's implied vol."""
+        a, b = _arr(inclSpots), _arr(inclTimes)
+        k, m = _arr(strikes), _arr(mats)
+        nS, nT = ctypes.c_int(), ctypes.c_int()
+        _check(lib().cf_dupire_calib(self._h, ctypes.byref(ivs), _p(a), len(a), ctypes.c_double(maxDs), _p(b), len(b),
+                                     ctypes.c_double(maxDtVol), ctypes.byref(nS), ctypes.byref(nT), None, None, None))
+        mb = _arr(micro).reshape(-1)
+        if mb.size != nS.value * nT.value:
+            raise CfError(-1, "calibAdjoint: micro must hold nS x nT local-vol adjoints")
+        vega = np.zeros(len(k) * len(m))
+        calls = np.zeros(nT.value * nS.value * 5)
+        cvegas = np.zeros(nT.value * nS.value * 5)
+        padj = np.zeros(nT.value * nS.value * 5)
+        _check(lib().cf_calib_adjoint(self._h, ctypes.byref(ivs), _p(a), len(a), ctypes.c_double(maxDs), _p(b), len(b),
+                                      ctypes.c_double(maxDtVol), _p(k), len(k), _p(m), len(m), _p(mb),
+                                      int(bool(refSeeding)), _p(vega), _p(calls), _p(cvegas), _p(padj)))
+        shape = (nT.value, nS.value, 5)
+        return dict(vega=vega.reshape(len(k), len(m)), calls=calls.reshape(shape), callVegas=cvegas.reshape(shape),
+                    pointAdj=padj.reshape(shape))
+
     # ---- RNG access --------------------------------------------------------------------------
     def dupireSuperbucketBump(self, ivs, spot, maxDt, productId, notionals, inclSpots, maxDs, inclTimes, maxDtVol,
                               strikes, mats, num, vegaBump=0.0):

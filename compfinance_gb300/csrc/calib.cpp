@@ -34,6 +34,7 @@ struct CalibRun
     std::vector<int> il, ih;
     DevBuf buf;
     CalibParams P;
+    double* pointAdjBuf = nullptr;  // room for the per-point adjoints of the test hook
 };
 
 // Grid (fillData) and the +-2.5 std window of each maturity (mcMdlDupire.h:299-312) on the
@@ -64,7 +65,7 @@ int calibrate(Context& c, const cf_ivs& ivs, const double* inclSpots, int nIS, d
         r.ih[j] = ih;
     }
     const size_t n5 = size_t(nS) * nT * 5;
-    const size_t bytes = (nS + nT + nK + nM) * 8 + 2 * nT * 4 + 2 * n5 * 8 + size_t(nS) * nT * 16 +
+    const size_t bytes = (nS + nT + nK + nM) * 8 + 2 * nT * 4 + 3 * n5 * 8 + size_t(nS) * nT * 16 +
                          size_t(nK) * nM * 24 + 4096;
     int rc = r.buf.ensure(bytes);
     if (rc) return rc;
@@ -90,6 +91,7 @@ int calibrate(Context& c, const cf_ivs& ivs, const double* inclSpots, int nIS, d
     int* dih = (int*)take(nT * 4);
     P.c = (double*)take(n5 * 8);
     P.vega = (double*)take(n5 * 8);
+    r.pointAdjBuf = (double*)take(n5 * 8);  // the test hook's per-point adjoints (P.pointAdj set there)
     P.lvT = (double*)take(size_t(nS) * nT * 8);
     double* dSeed = (double*)take(size_t(nS) * nT * 8);
     P.seed = dSeed;
@@ -113,8 +115,40 @@ int calibrate(Context& c, const cf_ivs& ivs, const double* inclSpots, int nIS, d
         (nM && cudaMemcpyAsync(dM, rvM, nM * 8, cudaMemcpyHostToDevice, s)) ||
         (spreads && cudaMemcpyAsync(dSp, spreads, size_t(nK) * nM * 8, cudaMemcpyHostToDevice, s)))
         return cuda_fail(cudaGetLastError(), "calibration upload");
+    // points outside each maturity's window are never priced: zero, for the readers of the calls
+    if (cudaMemsetAsync(P.c, 0, n5 * 8, s) != cudaSuccess || cudaMemsetAsync(P.vega, 0, n5 * 8, s) != cudaSuccess)
+        return cuda_fail(cudaGetLastError(), "calibration reset");
     rc = launch_calib(P, 0, s);
     if (rc) return cuda_fail(cudaError_t(rc), "calibration kernels");
+    return CF_OK;
+}
+
+// The calibration adjoint (the second half of main.h:519-562): local-vol adjoints micro[nS][nT]
+// -> d / d risk-view spread, vega[nK][nM].  A flat-extrapolated local vol is a copy of the edge
+// node of its maturity, so its adjoint belongs to that node: added (exact adjoint) or, with
+// refSeeding, assigned as the reference's seeding by assignment does (main.h:541-547).
+int calib_adjoint(Context& c, CalibRun& r, const double* micro, int refSeeding, double* vega)
+{
+    const int nS = r.P.nS, nT = r.P.nT, nK = r.P.nK, nM = r.P.nM;
+    std::vector<double> seed(size_t(nS) * nT, 0.0);
+    for (int i = 0; i < nS; ++i)
+        for (int j = 0; j < nT; ++j)
+        {
+            const int src = i < r.il[j] ? r.il[j] : i > r.ih[j] ? r.ih[j] : i;
+            double& sd = seed[size_t(src) * nT + j];
+            if (refSeeding) sd = micro[size_t(i) * nT + j];
+            else sd += micro[size_t(i) * nT + j];
+        }
+    cudaError_t e = cudaMemcpyAsync((void*)r.P.seed, seed.data(), seed.size() * 8, cudaMemcpyHostToDevice, c.stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(r.P.acc, 0, size_t(nK) * nM * 16, c.stream);
+    if (e != cudaSuccess) return cuda_fail(e, "calibration adjoint upload");
+    const int rc = launch_calib(r.P, 1, c.stream);
+    if (rc) return cuda_fail(cudaError_t(rc), "calibration adjoint");
+    std::vector<long long> acc(size_t(nK) * nM * 2);
+    e = cudaMemcpyAsync(acc.data(), r.P.acc, acc.size() * 8, cudaMemcpyDeviceToHost, c.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
+    if (e != cudaSuccess) return cuda_fail(e, "calibration adjoint fetch");
+    for (int k = 0; k < nK * nM; ++k) vega[k] = fix_value_host(acc[2 * k], acc[2 * k + 1]);
     return CF_OK;
 }
 
@@ -218,28 +252,39 @@ int cf_dupire_superbucket(cf_context* ctx, const cf_ivs* ivs, double spot, doubl
     *delta = risks[0];
     const double* micro = risks.data() + 1;
     if (microbucket) std::memcpy(microbucket, micro, size_t(nS) * nT * 8);
-    // 4. seeds of the calibration adjoint: a flat-extrapolated local vol is a copy of the
-    // edge node of its maturity, so its adjoint belongs to that node.
-    std::vector<double> seed(size_t(nS) * nT, 0.0);
-    for (int i = 0; i < nS; ++i)
-        for (int j = 0; j < nT; ++j)
-        {
-            const int src = i < r.il[j] ? r.il[j] : i > r.ih[j] ? r.ih[j] : i;
-            double& s = seed[size_t(src) * nT + j];
-            if (refSeeding) s = micro[size_t(i) * nT + j];  // main.h:541-547 assigns
-            else s += micro[size_t(i) * nT + j];
-        }
-    cudaError_t e = cudaMemcpyAsync((void*)r.P.seed, seed.data(), seed.size() * 8, cudaMemcpyHostToDevice, c.stream);
-    if (e == cudaSuccess) e = cudaMemsetAsync(r.P.acc, 0, size_t(nStrikes) * nMats * 16, c.stream);
-    if (e != cudaSuccess) return cuda_fail(e, "superbucket upload");
-    rc = launch_calib(r.P, 1, c.stream);
-    if (rc) return cuda_fail(cudaError_t(rc), "calibration adjoint");
-    std::vector<long long> acc(size_t(nStrikes) * nMats * 2);
-    e = cudaMemcpyAsync(acc.data(), r.P.acc, acc.size() * 8, cudaMemcpyDeviceToHost, c.stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
-    if (e != cudaSuccess) return cuda_fail(e, "superbucket fetch");
-    for (int k = 0; k < nStrikes * nMats; ++k) vega[k] = fix_value_host(acc[2 * k], acc[2 * k + 1]);
+    // 4. the calibration adjoint, seeded with the microbucket
+    if ((rc = calib_adjoint(c, r, micro, refSeeding, vega))) return rc;
     c.main.launches = 4;
+    return CF_OK;
+}
+
+int cf_calib_adjoint(cf_context* ctx, const cf_ivs* ivs, const double* inclSpots, int nInclSpots, double maxDs,
+                     const double* inclTimes, int nInclTimes, double maxDtVol, const double* strikes, int nStrikes,
+                     const double* mats, int nMats, const double* micro, int refSeeding, double* vega, double* calls,
+                     double* callVegas, double* pointAdj)
+{
+    if (!ctx || !ivs || !micro || !vega) return fail(CF_E_ARG, "null argument");
+    if (nStrikes < 1 || nMats < 1 || !strikes || !mats) return fail(CF_E_ARG, "calibration adjoint: empty risk view");
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    Context& c = ctx->c;
+    cudaSetDevice(c.device);
+    CalibRun r;
+    int rc = calibrate(c, *ivs, inclSpots, nInclSpots, maxDs, inclTimes, nInclTimes, maxDtVol, strikes, nStrikes,
+                       mats, nMats, r);
+    if (rc) return rc;
+    const size_t n5 = size_t(r.P.nS) * r.P.nT * 5;
+    r.P.pointAdj = pointAdj ? r.pointAdjBuf : nullptr;
+    cudaError_t e = cudaSuccess;
+    if (r.P.pointAdj) e = cudaMemsetAsync(r.P.pointAdj, 0, n5 * 8, c.stream);
+    if (e == cudaSuccess && calls) e = cudaMemcpyAsync(calls, r.P.c, n5 * 8, cudaMemcpyDeviceToHost, c.stream);
+    if (e == cudaSuccess && callVegas) e = cudaMemcpyAsync(callVegas, r.P.vega, n5 * 8, cudaMemcpyDeviceToHost, c.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
+    if (e != cudaSuccess) return cuda_fail(e, "calibration prices fetch");
+    int rc2 = calib_adjoint(c, r, micro, refSeeding, vega);
+    if (rc2 || !pointAdj) return rc2;
+    e = cudaMemcpyAsync(pointAdj, r.P.pointAdj, n5 * 8, cudaMemcpyDeviceToHost, c.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
+    if (e != cudaSuccess) return cuda_fail(e, "calibration point adjoints fetch");
     return CF_OK;
 }
 

@@ -202,6 +202,7 @@ __global__ void calib_adjoint_kernel(CalibParams p)
     const double dct = dsdu * 2.0 / ckk, dckk = -dsdu * 2.0 * ct / (ckk * ckk);
     const double dc = pt == 0 ? -2.0e08 * dckk : pt == 1 ? -0.5e04 * dct : pt == 2 ? 0.5e04 * dct : 1.0e08 * dckk;
     const double av = a * dc * p.vega[idx];
+    if (p.pointAdj) p.pointAdj[idx] = av;
     double Kp, Tp;
     fd_point(pt, K, p.times[j], Kp, Tp);
     int node[4];

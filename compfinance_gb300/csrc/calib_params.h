@@ -22,6 +22,7 @@ struct CalibParams
     const double* seed;   // [nS][nT] adjoint of each local vol (extrapolation folded in)
     const double* spreads;  // [nK][nM] risk-view spreads added to the implied vols, or null
     long long* acc;       // [nK*nM][2] fixed-point accumulators of d / d spread
+    double* pointAdj;     // [nT][nS][5] adjoint of each call's implied vol (test hook), or null
 };
 
 int launch_calib(const CalibParams& p, int adjoint, void* stream);

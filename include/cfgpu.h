@@ -197,6 +197,19 @@ int cf_dupire_superbucket_bump(cf_context* ctx, const cf_ivs* ivs, double spot, 
                                int nStrikes, const double* mats, int nMats, const cf_num_param* num, double vegaBump,
                                double* value, double* delta, double* vega);
 
+/* Test hook, no counterpart in the reference: the Dupire calibration's adjoint alone (the
+ * second half of dupireSuperbucket, main.h:519-562), seeded with local-vol adjoints
+ * micro[nS*nT] (spot-major, refSeeding as in cf_dupire_superbucket) instead of Monte Carlo
+ * ones: vega[nStrikes*nMats].  Per node and point, (K,T), (K,T-h), (K,T+h), (K-h,T), (K+h,T)
+ * with h = 1e-4, [nT*nS*5] each and optional: calls and callVegas receive the forward's
+ * Black-Scholes prices and their derivatives to the implied vol (the values Dupire's formula
+ * and its adjoint were taken at), pointAdj the adjoint of each point's implied vol before the
+ * risk view's interpolation spreads it; 0 outside each maturity's +-2.5 std window. */
+int cf_calib_adjoint(cf_context* ctx, const cf_ivs* ivs, const double* inclSpots, int nInclSpots, double maxDs,
+                     const double* inclTimes, int nInclTimes, double maxDtVol, const double* strikes, int nStrikes,
+                     const double* mats, int nMats, const double* micro, int refSeeding, double* vega,
+                     double* calls, double* callVegas, double* pointAdj);
+
 /* AADriskAggregate without any device allocation.  No counterpart in the reference.
  * For callers that cannot let a library allocate device memory during a call (memory
  * already reserved by another allocator, or a cudaMalloc / cudaFree stall is unacceptable):

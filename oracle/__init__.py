@@ -225,6 +225,41 @@ def calib_adjoint(iv, incl_spots, max_ds, incl_times, max_dt_vol, rv_strikes, rv
     return vega.reshape(len(k), len(m))
 
 
+def calib_adjoint_given(iv, incl_spots, max_ds, incl_times, max_dt_vol, rv_strikes, rv_mats, micro, calls=None,
+                        vegas=None, ref_quirk=False):
+    """The calibration adjoint restated pointwise: each node's five calls enter the tape as one
+    node of their implied vol, with the given values `calls` and partials `vegas` ([nT][nS][5],
+    per node (K,T), (K,T-h), (K,T+h), (K-h,T), (K+h,T)); None: the oracle's own.  Returns a dict:
+    vega [strike][mat]; calls, vegas (the oracle's own) and pointAdj (the adjoint of each point's
+    implied vol), [nT][nS][5]; absTerms [strike][mat], the sum of |pointAdj| x interpolation
+    weight over the points, the scale of the terms that cancel in vega."""
+    isp, pis = _arr(incl_spots)
+    itm, pit = _arr(incl_times)
+    k, pk = _arr(rv_strikes)
+    m, pm = _arr(rv_mats)
+    mb, pmb = _arr(np.asarray(micro).reshape(-1))
+    s, t, _lv = calib(iv, incl_spots, max_ds, incl_times, max_dt_vol)
+    n5 = len(s) * len(t) * 5
+    own, po = _arr(np.zeros(n5))
+    ownv, pov = _arr(np.zeros(n5))
+    padj, ppa = _arr(np.zeros(n5))
+    pc = pvg = None
+    if calls is not None:
+        c, pc = _arr(np.asarray(calls).reshape(-1))
+        assert c.size == n5
+    if vegas is not None:
+        vg, pvg = _arr(np.asarray(vegas).reshape(-1))
+        assert vg.size == n5
+    vega, pv = _arr(np.zeros(len(k) * len(m)))
+    absT, pab = _arr(np.zeros(len(k) * len(m)))
+    lib().orc_calib_adjoint_given(ctypes.byref(iv), pis, len(isp), ctypes.c_double(max_ds), pit, len(itm),
+                                  ctypes.c_double(max_dt_vol), pk, len(k), pm, len(m), pmb, int(ref_quirk), pc, pvg,
+                                  po, pov, ppa, pab, pv, 1)
+    shape = (len(t), len(s), 5)
+    return dict(vega=vega.reshape(len(k), len(m)), calls=own.reshape(shape), vegas=ownv.reshape(shape),
+                pointAdj=padj.reshape(shape), absTerms=absT.reshape(len(k), len(m)))
+
+
 def superbucket(iv, spot, maxdt, product, notionals, incl_spots, max_ds, incl_times, max_dt_vol,
                 rv_strikes, rv_mats, sobol, npath, seed1=12345, seed2=1234, ref_quirk=False):
     isp, pis = _arr(incl_spots)

@@ -15,6 +15,7 @@
 #include <memory>
 #include <string>
 #include <thread>
+#include <type_traits>
 #include <vector>
 
 namespace {
@@ -1125,6 +1126,51 @@ T localVol(const orc_ivs& s, double K, double mat, const RiskViewT<T>* rv)
     return sqrt(2.0 * ct / ckk) / K;
 }
 
+// d blackScholes / d vol by the tape's rules (normalCdf' = normalDens, AADExpr.h:434-447), on a
+// tape of its own.
+double bsVegaTape(double spot, double K, double vol, double mat)
+{
+    Tape* outer = gTape;
+    Tape t;
+    gTape = &t;
+    const Var v = leaf(vol);
+    const Var c = blackScholes<Var>(spot, K, v, mat);
+    t.sizeAdj();
+    if (c.i >= 0)
+    {
+        t.adj[size_t(c.i)] = 1.0;
+        t.sweep(t.nodes.size(), 0);
+    }
+    const double d = t.adj[size_t(v.i)];
+    gTape = outer;
+    return d;
+}
+
+// IVS::localVol (ivs.h:119-138) on the tape with each of its five calls recorded as one node of
+// its implied vol (plus the risk view's spread): value c and partial d c / d vol, the oracle's
+// own (own, ownV receive them) or given ones.  Dupire's formula and its partials are then taken at
+// those values.  The points are, in this order, (K,T), (K,T-h), (K,T+h), (K-h,T), (K+h,T), h = 1e-4.
+Var localVolPoints(const orc_ivs& s, double K, double mat, const RiskViewT<Var>* rv, const double* given,
+                   const double* givenV, double* own, double* ownV, int* volNode)
+{
+    const double Kp[5] = {K, K, K, K - 1.0e-04, K + 1.0e-04};
+    const double Tp[5] = {mat, mat - 1.0e-04, mat + 1.0e-04, mat, mat};
+    Var c[5];
+    for (int k = 0; k < 5; ++k)
+    {
+        const Var vol = impliedVol(s, Kp[k], Tp[k]) + rv->spread(Kp[k], Tp[k]);
+        const double cv = blackScholes<double>(s.spot, Kp[k], vol.v, Tp[k]);
+        const double dv = bsVegaTape(s.spot, Kp[k], vol.v, Tp[k]);
+        if (own) own[k] = cv;
+        if (ownV) ownV[k] = dv;
+        c[k] = un(given ? given[k] : cv, vol, givenV ? givenV[k] : dv);
+        if (volNode) volNode[k] = vol.i;
+    }
+    const Var ct = (c[2] - c[1]) * 0.5e04;
+    const Var ckk = (c[3] + c[4] - 2.0 * c[0]) * 1.0e08;
+    return sqrt(2.0 * ct / ckk) / K;
+}
+
 struct CalibGrid
 {
     vector<double> spots, times;
@@ -1138,9 +1184,18 @@ CalibGrid calibGrid(const double* inclSpots, int nIS, double maxDs, const double
     return g;
 }
 
-// lvols spot-major [nS][nT]
+// The five calls and vegas of each node for localVolPoints, at [(j nS + i) 5, +5) of each array
+// (node: spot i, time j); null arrays: the oracle's own values, not recorded.
+struct CalibPoints
+{
+    const double *calls, *vegas;
+    double *ownCalls, *ownVegas;
+    int* volNode;  // tape node of each point's implied vol
+};
+
+// lvols spot-major [nS][nT]; with points (T = Var) each node through localVolPoints
 template <class T>
-vector<T> calibrate(const orc_ivs& s, const CalibGrid& g, const RiskViewT<T>& rv)
+vector<T> calibrate(const orc_ivs& s, const CalibGrid& g, const RiskViewT<T>& rv, const CalibPoints* points = nullptr)
 {
     const size_t nS = g.spots.size(), nT = g.times.size();
     vector<T> lv(nS * nT);
@@ -1153,7 +1208,19 @@ vector<T> calibrate(const orc_ivs& s, const CalibGrid& g, const RiskViewT<T>& rv
         while (il < int(nS) && g.spots[il] < s.spot - 2.5 * sd) ++il;
         int ih = int(nS) - 1;
         while (ih >= 0 && g.spots[ih] > s.spot + 2.5 * sd) --ih;
-        for (int i = il; i <= ih; ++i) lv[i * nT + j] = localVol<T>(s, g.spots[i], mat, &rv);
+        for (int i = il; i <= ih; ++i)
+        {
+            if constexpr (std::is_same_v<T, Var>)
+                if (points)
+                {
+                    const size_t c5 = (j * nS + size_t(i)) * 5;
+                    auto at = [&](auto* a) { return a ? a + c5 : nullptr; };
+                    lv[i * nT + j] = localVolPoints(s, g.spots[i], mat, &rv, at(points->calls), at(points->vegas),
+                                                    at(points->ownCalls), at(points->ownVegas), at(points->volNode));
+                    continue;
+                }
+            lv[i * nT + j] = localVol<T>(s, g.spots[i], mat, &rv);
+        }
         for (int i = 0; i < il; ++i) lv[i * nT + j] = lv[il * nT + j];
         for (int i = ih + 1; i < int(nS); ++i) lv[i * nT + j] = lv[ih * nT + j];
     }
@@ -1688,6 +1755,16 @@ int orc_calib_adjoint(const orc_ivs* ivs, const double* inclSpots, int nIS, doub
                       int nIT, double maxDtVol, const double* rvK, int nK, const double* rvM, int nM,
                       const double* micro, int refSeedQuirk, double* vega)
 {
+    return orc_calib_adjoint_given(ivs, inclSpots, nIS, maxDs, inclTimes, nIT, maxDtVol, rvK, nK, rvM, nM, micro,
+                                   refSeedQuirk, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, vega, 0);
+}
+
+int orc_calib_adjoint_given(const orc_ivs* ivs, const double* inclSpots, int nIS, double maxDs,
+                            const double* inclTimes, int nIT, double maxDtVol, const double* rvK, int nK,
+                            const double* rvM, int nM, const double* micro, int refSeedQuirk, const double* calls,
+                            const double* vegas, double* ownCalls, double* ownVegas, double* pointAdj,
+                            double* absTerms, double* vega, int pointwise)
+{
     Tape tape;
     gTape = &tape;
     const CalibGrid g = calibGrid(inclSpots, nIS, maxDs, inclTimes, nIT, maxDtVol);
@@ -1696,7 +1773,12 @@ int orc_calib_adjoint(const orc_ivs* ivs, const double* inclSpots, int nIS, doub
     rv.strikes.assign(rvK, rvK + nK);
     rv.mats.assign(rvM, rvM + nM);
     for (int i = 0; i < nK * nM; ++i) rv.spreads.push_back(leaf(0.0));
-    const auto lv = calibrate<Var>(*ivs, g, rv);
+    const size_t n5 = g.spots.size() * g.times.size() * 5;
+    if (ownCalls) std::fill(ownCalls, ownCalls + n5, 0.0);
+    if (ownVegas) std::fill(ownVegas, ownVegas + n5, 0.0);
+    vector<int> volNode(n5, -1);
+    const CalibPoints pts{calls, vegas, ownCalls, ownVegas, volNode.data()};
+    const auto lv = calibrate<Var>(*ivs, g, rv, pointwise ? &pts : nullptr);
     tape.width = 1;
     tape.sizeAdj();
     // Flat-extrapolated local vols are copies of the edge node (mcMdlDupire.h:320-324), so the
@@ -1710,6 +1792,24 @@ int orc_calib_adjoint(const orc_ivs* ivs, const double* inclSpots, int nIS, doub
         }
     tape.sweep(tape.nodes.size(), 0);
     for (int i = 0; i < nK * nM; ++i) vega[i] = tape.adj[size_t(rv.spreads[i].i)];
+    if (pointwise && (pointAdj || absTerms))
+    {
+        // the adjoint of each point's implied vol; then, per spread node, the sum over points of
+        // |that adjoint| x the point's interpolation weight on the node (the weights are >= 0): a
+        // second sweep seeded with the absolute point adjoints only
+        vector<double> pa(n5, 0.0);
+        for (size_t k = 0; k < n5; ++k)
+            if (volNode[k] >= 0) pa[k] = tape.adj[size_t(volNode[k])];
+        if (pointAdj) std::copy(pa.begin(), pa.end(), pointAdj);
+        if (absTerms)
+        {
+            std::fill(tape.adj.begin(), tape.adj.end(), 0.0);
+            for (size_t k = 0; k < n5; ++k)
+                if (volNode[k] >= 0) tape.adj[size_t(volNode[k])] += std::fabs(pa[k]);
+            tape.sweep(tape.nodes.size(), 0);
+            for (int i = 0; i < nK * nM; ++i) absTerms[i] = tape.adj[size_t(rv.spreads[i].i)];
+        }
+    }
     gTape = nullptr;
     return 0;
 }

@@ -104,6 +104,21 @@ int orc_calib_adjoint(const orc_ivs* ivs, const double* inclSpots, int nIS, doub
                       int nK, const double* rvMats, int nM, const double* microbucket,
                       int refSeedQuirk, double* vega);
 
+/* The same adjoint, restated pointwise (pointwise != 0): each of a node's five calls, (K,T),
+ * (K,T-h), (K,T+h), (K-h,T), (K+h,T) with h = 1e-4, enters the tape as one node of its implied
+ * vol with value c and partial d c / d vol.  calls / vegas ([nT][nS][5], NULL: the oracle's own)
+ * give them, so that Dupire's formula, its partials, the risk view's interpolation weights and
+ * the seeding are restated at those values.  Optional outputs, [nT][nS][5] (0 outside the
+ * +-2.5 std window): ownCalls / ownVegas the oracle's own values, pointAdj the adjoint of each
+ * point's implied vol; absTerms[nK*nM]: per spread node, the sum over points of |pointAdj| x the
+ * point's interpolation weight on the node (the scale of the terms summed into vega).
+ * pointwise == 0: the full tape of orc_calib_adjoint. */
+int orc_calib_adjoint_given(const orc_ivs* ivs, const double* inclSpots, int nIS, double maxDs,
+                            const double* inclTimes, int nIT, double maxDtVol, const double* rvStrikes,
+                            int nK, const double* rvMats, int nM, const double* microbucket,
+                            int refSeedQuirk, const double* calls, const double* vegas, double* ownCalls,
+                            double* ownVegas, double* pointAdj, double* absTerms, double* vega, int pointwise);
+
 /* dupireSuperbucket: value, delta, vega[nK*nM]; microbucket[nS*nT] optional. */
 int orc_superbucket(const orc_ivs* ivs, double spot, double maxDt, const orc_product* p,
                     const double* notionals, const double* inclSpots, int nIS, double maxDs,

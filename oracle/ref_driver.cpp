@@ -596,6 +596,11 @@ int main()
                 put("sb_microbucket", std::vector<double>(mc.vega.begin(),
                     mc.vega.begin() + mc.vega.rows() * mc.vega.cols()));
                 put("sb_vega", vega);
+                // the calibrated model the Monte Carlo adjoints were taken on
+                put("sb_spots", calib.spots);
+                put("sb_times", calib.times);
+                put("sb_lvols", std::vector<double>(calib.lVols.begin(),
+                    calib.lVols.begin() + calib.lVols.rows() * calib.lVols.cols()));
             }
             double t1 = now_s();
             put("seconds", {t1 - t0});

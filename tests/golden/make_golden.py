@@ -7,7 +7,7 @@ AADriskAggregate, AADriskMulti, bumpRisk, dupireCalib, dupireSuperbucket, the RN
 Every case records its inputs next to its outputs, so the fixtures are self-contained:
 the tests never need the reference.
 
-    python3 tests/golden/make_golden.py [rng host mc calib bump products multi_asset]   # all when none named;
+    python3 tests/golden/make_golden.py [rng host mc calib bump products multi_asset baseline]   # all when none named;
                                                                    # rebuilds the driver when missing
                                                                    # (from CF_REFERENCE_DIR)
 """
@@ -520,10 +520,43 @@ def calib_cases():
                    sobol=1, npath=npath, value=d["sb_value"][0], delta=d["sb_delta"][0], vega=d["sb_vega"])
         if "sb_microbucket" in d:
             rec["microbucket"] = d["sb_microbucket"]
+            rec["lvol_spots"], rec["lvol_times"], rec["lvols"] = d["sb_spots"], d["sb_times"], d["sb_lvols"]
         sbs.append(rec)
     out["superbucket"] = sbs
     r = run([f"analytics {f(100.0)} {f(110.0)} {f(0.2)} {f(1.5)} {f(0.03)} {f(0.01)} {f(140.0)}"])
     out["analytics"] = dict(inputs=[100.0, 110.0, 0.2, 1.5, 0.03, 0.01, 140.0], out=r[0][1])
+    return out
+
+
+def baseline_cases(models, products):
+    """The benchmark's own configurations through the reference: the 60x30 Dupire barrier's
+    AADriskOne at 2^18 mrg32k3a paths (1801 risks), and the superbucket of the 200-European
+    portfolio (parametric implied surface, 60x30 local vols, 30x12 risk view, 36 monthly steps)
+    at 2^20 Sobol paths, with the reference's calibrated local vols and microbucket."""
+    out = {}
+    m = models["dup60x30"]
+    cmds = [model_cmd("dup60x30", m), product_cmd("uoc", products["uoc"]),
+            f"risk dup60x30 uoc {num(0, 1 << 18, par=1)} 0"]
+    r = run(cmds)
+    out["c2"] = dict(model="dup60x30", product="uoc", mode="risk", sobol=0, npath=1 << 18, seed1=12345, seed2=1234,
+                     payoff=0, values=r[0][1], risk_value=r[1][1][0], risks=r[2][1])
+    iv = W.SB_IVS
+    ivs = f"param {f(100.0)} {f(iv['a'])} {f(iv['b'])} {f(iv['c'])} {f(iv['sref'])}"
+    isp, mds, itm, mdt = W.superbucket_grid(60, 30)
+    rk, rm = W.superbucket_riskview(30, 12)
+    mats, strikes = W.superbucket_portfolio(10, 20)
+    nots = [(k, 1.0) for k in range(len(mats))]
+    cmds = [cmd_europeans("c4port", mats, strikes),
+            f"superbucket {ivs} {len(isp)} {fl(isp)} {f(mds)} {len(itm)} {fl(itm)} {f(mdt)} {f(1.0 / 12.0)} c4port "
+            f"{len(nots)} " + " ".join(f"{k} {f(w)}" for k, w in nots) +
+            f" {len(rk)} {fl(rk)} {len(rm)} {fl(rm)} {num(1, 1 << 20, par=1)}"]
+    d = {tag: v for tag, v in run(cmds)}
+    out["c4"] = dict(ivs="param", ivs_params=[100.0, iv["a"], iv["b"], iv["c"], iv["sref"]], incl_spots=isp,
+                     max_ds=mds, incl_times=itm, max_dt_vol=mdt, maxdt=1.0 / 12.0,
+                     portfolio=dict(mats=mats, strikes=strikes), notionals=nots, rv_strikes=rk, rv_mats=rm,
+                     sobol=1, npath=1 << 20, value=d["sb_value"][0], delta=d["sb_delta"][0], vega=d["sb_vega"],
+                     microbucket=d["sb_microbucket"], lvol_spots=d["sb_spots"], lvol_times=d["sb_times"],
+                     lvols=d["sb_lvols"])
     return out
 
 
@@ -533,7 +566,8 @@ def main():
     for name, fn in [("rng", rng_cases), ("host", lambda: host_cases(models, products)),
                      ("mc", lambda: mc_cases(models, products)), ("calib", calib_cases),
                      ("bump", lambda: bump_cases(models, products)), ("products", lambda: product_cases(models)),
-                     ("multi_asset", multi_asset_cases)]:
+                     ("multi_asset", multi_asset_cases),
+                     ("baseline", lambda: baseline_cases(models, products))]:
         if only and name not in only:
             continue
         obj = fn()

@@ -6,6 +6,7 @@ import pytest
 import oracle as O
 from compfinance_gb300 import Engine
 from compfinance_gb300 import workloads as W
+from calib_util import support as _support
 from gpu_util import num, rel_to_max
 
 pytestmark = pytest.mark.gpu
@@ -151,6 +152,95 @@ def test_superbucket_vs_reference_and_oracle(eng, golden, which):
                             c["rv_mats"], ex["microbucket"])
     print(which, "adjoint vs oracle", rel_to_max(ex["vega"], ovega))
     assert rel_to_max(ex["vega"], ovega) < 1e-2
+
+
+def _sb_case(golden, which):
+    if which == "c4":
+        return golden("baseline")["c4"]
+    return [x for x in golden("calib")["superbucket"] if x["name"] == which][0]
+
+
+@pytest.mark.parametrize("which", ["sb_param", "sb_merton", "c4"])
+@pytest.mark.parametrize("ref_seeding", [True, False])
+def test_calibration_adjoint_tight_vs_oracle_tape(eng, golden, which, ref_seeding):
+    """The calibration adjoint alone (main.h:519-562), pinned tightly against the oracle's tape.
+
+    Per node, Dupire's formula takes a second difference of 5 Black-Scholes prices divided by
+    1e-8.  In the adjoint, the 5 points' terms, spread onto the risk view with nearly equal
+    smoothstep weights, cancel: each vega entry is a sum of terms up to ~5e10 times the largest
+    entry.  So the adjoint moves by ~3e-3 of its largest entry under a 1e-15 relative change of
+    the prices, and two evaluation orders of the same sum agree only to a few ulps of its terms.
+    The check is therefore split:
+      * the forward values the adjoint is taken at (the 5 prices per node and their derivatives
+        to the implied vol), where nothing cancels: GPU against oracle to 1e-13;
+      * the adjoint of each point's implied vol (Dupire's partials, the seeding of the
+        extrapolated nodes, at the GPU's forward values), where nothing cancels either: 1e-12;
+      * each vega entry (the risk view's interpolation and the sums): to rounding, i.e. within
+        1e-13 of the sum of the absolute values of its terms plus 1e-15 of the absolute point
+        adjoints of the interpolation cells it is a corner of (see _support).
+    Seeds: the reference's own microbucket where the fixture has one (param surface, C4), else
+    seeded random adjoints (Merton surface)."""
+    c = _sb_case(golden, which)
+    iv = Engine.ivs(c["ivs"], c["ivs_params"][0], c["ivs_params"][1:])
+    oiv = O.ivs(c["ivs"], c["ivs_params"][0], c["ivs_params"][1:])
+    grid = (c["incl_spots"], c["max_ds"], c["incl_times"], c["max_dt_vol"])
+    s, t, _ = O.calib(oiv, *grid)
+    if "microbucket" in c:
+        micro = np.array(c["microbucket"])
+    else:
+        micro = np.random.RandomState(41).standard_normal(len(s) * len(t))
+    g = eng.calibAdjoint(iv, *grid, c["rv_strikes"], c["rv_mats"], micro, refSeeding=ref_seeding)
+    o = O.calib_adjoint_given(oiv, *grid, c["rv_strikes"], c["rv_mats"], micro, calls=g["calls"],
+                              vegas=g["callVegas"], ref_quirk=ref_seeding)
+    assert np.array_equal(g["calls"] == 0.0, o["calls"] == 0.0)
+    assert rel_to_max(g["calls"], o["calls"]) < 1e-13
+    assert rel_to_max(g["callVegas"], o["vegas"]) < 1e-13
+    assert np.abs(o["pointAdj"]).max() > 0
+    assert rel_to_max(g["pointAdj"], o["pointAdj"]) < 1e-12
+    bound = 1e-13 * o["absTerms"] + 1e-15 * _support(s, t, c["rv_strikes"], c["rv_mats"], o["pointAdj"])
+    diff = np.abs(g["vega"] - o["vega"])
+    print(which, ref_seeding, "point adjoints", rel_to_max(g["pointAdj"], o["pointAdj"]), "vega diff / bound",
+          (diff / np.maximum(bound, 1e-300)).max(), "vega rel to max", rel_to_max(g["vega"], o["vega"]))
+    assert np.all(diff <= bound)
+    assert np.abs(o["vega"]).max() > 0
+
+
+@pytest.mark.parametrize("which", ["sb_param", "c4"])
+def test_microbucket_on_reference_local_vols(eng, golden, which):
+    """The Monte Carlo half of the superbucket on the reference's own calibrated local vols: the
+    book value, delta and microbucket (adjoints to every local vol) of the reference's
+    dupireAADRisk on the same Sobol paths, to 1e-12 (C4: 200 Europeans, 36 monthly steps,
+    60x30 local vols, 2^20 paths).  With the microbucket equal, the calibration adjoint of it
+    is pinned by the test above: the remaining differences of the end-to-end vega from the
+    reference's come from the local vols' own rounding noise."""
+    c = _sb_case(golden, which)
+    s, t = np.array(c["lvol_spots"]), np.array(c["lvol_times"])
+    lv = np.array(c["lvols"]).reshape(len(s), len(t))
+    eng.putDupire(100.0, s, t, lv, c["maxdt"], f"reflv_{which}")
+    eng.putEuropeans(c["portfolio"]["mats"], c["portfolio"]["strikes"], f"refport_{which}")
+    w = np.zeros(len(c["portfolio"]["mats"]))
+    for k, x in c["notionals"]:
+        w[k] = x
+    r = eng.AADriskAggregate(f"reflv_{which}", f"refport_{which}", w, num(1, c["npath"]))
+    assert abs(r["riskPayoffValue"] - c["value"]) <= 1e-12 * abs(c["value"])
+    assert abs(r["risks"][0] - c["delta"]) <= 1e-12 * abs(c["delta"])
+    assert rel_to_max(r["risks"][1:], c["microbucket"]) < 1e-12
+
+
+def test_c4_superbucket_end_to_end_vs_reference(eng, golden):
+    """The whole C4 chain on the GPU (calibration, 2^20 Sobol paths of Monte Carlo adjoints,
+    calibration adjoint) against the reference's: value and delta to the local vols' rounding
+    noise; vega within the loose end-to-end bound of that noise (the tight checks are above)."""
+    c = golden("baseline")["c4"]
+    iv = Engine.ivs(c["ivs"], c["ivs_params"][0], c["ivs_params"][1:])
+    eng.putEuropeans(c["portfolio"]["mats"], c["portfolio"]["strikes"], "c4e2e")
+    w = np.ones(len(c["portfolio"]["mats"]))
+    r = eng.dupireSuperbucket(iv, 100.0, c["maxdt"], "c4e2e", w, c["incl_spots"], c["max_ds"], c["incl_times"],
+                              c["max_dt_vol"], c["rv_strikes"], c["rv_mats"], num(1, c["npath"]), refSeeding=True)
+    print("c4", r["value"] - c["value"], r["delta"] - c["delta"], rel_to_max(r["vega"], c["vega"]))
+    assert abs(r["value"] - c["value"]) < 1e-4 * abs(c["value"])
+    assert abs(r["delta"] - c["delta"]) < 1e-3 * abs(c["delta"])
+    assert rel_to_max(r["vega"], c["vega"]) < 5e-2
 
 
 def test_superbucket_finite_differences(eng):

@@ -277,6 +277,31 @@ def test_tma_staged_local_vols_bit_identical(eng, monkeypatch, precision):
     assert np.abs(out["1"]["risks"]).max() > 0
 
 
+def test_c2_risk_at_full_size_vs_reference(eng, golden):
+    """The 60x30 barrier's AADriskOne at its configured 2^18 mrg32k3a paths against the
+    reference's own run (value and all 1801 risks): FP64 to 1e-12; the FP32 form within 0.1
+    Monte Carlo standard error of the reference (standard errors from 8 independent runs of a
+    quarter of the paths)."""
+    d = golden("mc")
+    c = golden("baseline")["c2"]
+    put_model(eng, "c2full", d["models"][c["model"]])
+    put_product(eng, "c2uoc", d["products"][c["product"]])
+    r64 = eng.AADriskOne("c2full", "c2uoc", num(0, c["npath"]))
+    assert rel_to_max(r64["payoffValues"], c["values"]) < TOL
+    assert abs(r64["riskPayoffValue"] - c["risk_value"]) <= TOL * abs(c["risk_value"])
+    assert rel_to_max(r64["risks"], c["risks"]) < TOL
+    runs = np.array([eng.AADriskOne("c2full", "c2uoc", num(0, c["npath"] // 4, "fp64", 500 + k, 60 + k))["risks"]
+                     for k in range(8)])
+    se = runs.std(axis=0, ddof=1) / 2.0
+    vse = eng.value("c2full", "c2uoc", num(0, c["npath"]))["stderrs"][0]
+    r32 = eng.AADriskOne("c2full", "c2uoc", num(0, c["npath"], "fp32"))
+    assert abs(r32["payoffValues"][0] - c["values"][0]) <= 0.1 * vse
+    ref = np.array(c["risks"])
+    mask = se > 1e-6 * np.abs(ref).max()
+    assert np.all(np.abs(r32["risks"] - ref)[mask] <= 0.1 * se[mask])
+    assert np.all(np.abs(r32["risks"] - ref)[~mask] <= 1e-6 * np.abs(ref).max())
+
+
 @pytest.mark.parametrize("grid", [(20, 10), (60, 30), (120, 60)])
 def test_fp32_risk_rows_staged_bit_identical(eng, monkeypatch, grid):
     """The FP32 risk kernel with its forward's local-vol rows staged into shared memory by bulk

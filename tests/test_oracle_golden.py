@@ -6,6 +6,7 @@ import numpy as np
 import pytest
 
 import oracle as O
+from calib_util import support
 
 
 def rel(a, b):
@@ -161,6 +162,47 @@ def test_superbucket(golden):
         if "microbucket" in c:
             assert rel(mb, c["microbucket"]) < 1e-13
         assert rel(vega, c["vega"]) < 2e-5, c["name"]
+
+
+def test_calibration_adjoint_pointwise(golden):
+    """The pointwise restatement of the calibration adjoint (each call one tape node of its implied
+    vol, with value and partial): at given values equal to its own, bit for bit what it computes
+    alone; against the full tape adjoint, to rounding of the terms it sums (each vega entry is a
+    sum of terms up to ~5e10 times the largest entry, which cancel); against the reference's
+    superbucket vega on the reference's microbucket, within the same rounding."""
+    for c in golden("calib")["superbucket"]:
+        iv = O.ivs(c["ivs"], c["ivs_params"][0], c["ivs_params"][1:])
+        grid = (c["incl_spots"], c["max_ds"], c["incl_times"], c["max_dt_vol"])
+        s, t, _ = O.calib(iv, *grid)
+        micro = np.random.RandomState(3).standard_normal(len(s) * len(t))
+        for q in (False, True):
+            v0 = O.calib_adjoint(iv, *grid, c["rv_strikes"], c["rv_mats"], micro, ref_quirk=q)
+            r1 = O.calib_adjoint_given(iv, *grid, c["rv_strikes"], c["rv_mats"], micro, ref_quirk=q)
+            r2 = O.calib_adjoint_given(iv, *grid, c["rv_strikes"], c["rv_mats"], micro, calls=r1["calls"],
+                                       vegas=r1["vegas"], ref_quirk=q)
+            assert np.array_equal(r1["vega"], r2["vega"]), c["name"]
+            assert np.all(np.abs(r1["vega"] - v0) <= 1e-13 * r1["absTerms"]), c["name"]
+            assert (r1["calls"] > 0).any() and (r1["vegas"] > 0).any()
+        if "microbucket" in c:
+            r = O.calib_adjoint_given(iv, *grid, c["rv_strikes"], c["rv_mats"], c["microbucket"], ref_quirk=True)
+            ref = np.array(c["vega"]).reshape(r["vega"].shape)
+            assert np.all(np.abs(r["vega"] - ref) <= 1e-13 * r["absTerms"]), c["name"]
+
+
+def test_calibration_adjoint_pointwise_c4(golden):
+    """The same restatement on the superbucket workload (60x30 local vols, 30x12 risk view), seeded
+    with the reference's microbucket at 2^20 paths, against the reference's vega: within rounding
+    of the terms and of the risk view's interpolation weights (a calibration time one ulp below a
+    risk-view maturity gives a corner weight of 0 exactly or ~1e-16, on point adjoints ~1e11)."""
+    c = golden("baseline")["c4"]
+    iv = O.ivs(c["ivs"], c["ivs_params"][0], c["ivs_params"][1:])
+    grid = (c["incl_spots"], c["max_ds"], c["incl_times"], c["max_dt_vol"])
+    s, t, _ = O.calib(iv, *grid)
+    r = O.calib_adjoint_given(iv, *grid, c["rv_strikes"], c["rv_mats"], c["microbucket"], ref_quirk=True)
+    ref = np.array(c["vega"]).reshape(r["vega"].shape)
+    bound = 1e-13 * r["absTerms"] + 1e-15 * support(s, t, c["rv_strikes"], c["rv_mats"], r["pointAdj"])
+    assert np.all(np.abs(r["vega"] - ref) <= bound)
+    assert rel(r["vega"], ref) < 1e-5
 
 
 def test_contingent_bond(golden):

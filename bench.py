@@ -36,8 +36,12 @@ METRIC = "AAD-risk paths/s (Dupire barrier), FP32 vs FP64 at equal error; serve 
 NPATH = 1 << 22
 GRID = (60, 30)
 FLOPS_PER_PATH_STEP = 53.0   # algorithmic FP work of value + adjoint per path-step (mrg32k3a)
-TRAFFIC_BYTES_PER_PATH_STEP = 11.79  # measured DRAM traffic of the FP32 risk launch per path-step
-INST_PER_PATH_STEP = 107.5  # measured thread instructions of the FP32 risk launch per path-step
+TRAFFIC_BYTES_PER_PATH_STEP = 11.72  # measured DRAM traffic of the FP32 risk launch per path-step
+INST_PER_PATH_STEP = 108.2  # measured thread instructions of the FP32 risk launch per path-step
+# FP64 form (mc_kernel<double>): ncu of the same kernel at 2^18 paths measures its FP64 pipe 82.9%
+# busy; GB300 executes 2 FP64 FMAs per SM per cycle (ncu's peak of the DFMA counter)
+FP64_PIPE_BUSY_NCU = 0.829
+DFMA_PER_SM_PER_CYCLE = 2
 CONFIG = {
     "workload": "dupire_uoc_aad_risk_60x30_156steps_2^22paths_fp32path",
     "model": "Dupire local vol 60x30 (50-200 log-spaced x 0.1-3.0y), seeded synthetic surface",
@@ -363,8 +367,15 @@ def run_reference(args):
 def run_case(args):
     """One secondary workload alone, for profiler captures: `--case multi` is AADriskMulti of the
     superbucket portfolio (200 Europeans, 36 monthly steps, Sobol) on a synthetic Dupire grid;
-    `--case autocall|basket` is AADriskOne of the four-asset autocall or basket (Sobol)."""
+    `--case autocall|basket` is AADriskOne of the four-asset autocall or basket (Sobol);
+    `--case superbucket` the whole dupireSuperbucket chain of the portfolio (calibration of the
+    parametric surface to 60x30 local vols, Monte Carlo adjoints, calibration adjoint to 30x12)."""
     paths = args.paths if args.paths != NPATH else 1 << 20
+    if args.case == "superbucket":
+        sec = W.run_superbucket(paths, args.reps, args.precision)
+        print(f"dupireSuperbucket 30x12 -> 60x30, 200 Europeans, {args.precision} {paths} paths: "
+              f"{1e3 * sec:.3f} ms per call")
+        return 0
     if args.case == "multi":
         g = tuple(int(x) for x in args.grid.split("x"))
         sec = W.run_multi(g, paths, args.reps, args.precision)
@@ -389,9 +400,10 @@ def main():
     ap.add_argument("--serve-requests", type=int, default=10000)
     ap.add_argument("--paths", type=int, default=NPATH,
                     help="paths per step (default 2^22; smaller cases are for profiler captures only)")
-    ap.add_argument("--case", choices=["multi", "autocall", "basket"],
+    ap.add_argument("--case", choices=["multi", "autocall", "basket", "superbucket"],
                     help="time one secondary workload alone (for profiler captures) and exit: the superbucket "
-                         "portfolio's AADriskMulti, or AADriskOne of the four-asset autocall or basket")
+                         "portfolio's AADriskMulti, AADriskOne of the four-asset autocall or basket, or the whole "
+                         "dupireSuperbucket chain of that portfolio")
     ap.add_argument("--grid", default="60x30", help="--case multi: local-vol grid")
     ap.add_argument("--reps", type=int, default=1, help="--case: timed calls after one warm-up call")
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"], help="--case: path precision")
@@ -505,6 +517,7 @@ def main():
     pk = peaks()
     sm_max = float(pk.get("sm_max_mhz", 2070.0))
     peak_fp32 = 152 * 128 * 2 * sm_max * 1e6 / 1e12
+    peak_fp64 = 152 * DFMA_PER_SM_PER_CYCLE * 2 * sm_max * 1e6 / 1e12
     achieved = FLOPS_PER_PATH_STEP * steps_tot / per_step / 1e12
     # DRAM bytes per launch: dram__bytes_read.sum + dram__bytes_write.sum of one ncu capture of
     # dupire_risk32 at 2^20 paths, per path-step, times the path-steps of this launch (same grid,
@@ -516,7 +529,16 @@ def main():
         "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config,
         "path_steps_per_s": value * dim,
         "fp64": {"value": world * npath / (t64 / steps64), "unit": "paths/s", "ms_per_step": t64 / steps64 * 1e3,
-                 "steps": steps64},
+                 "steps": steps64,
+                 # the same 53 algorithmic flops per path-step against the FP64 FMA peak; the kernel's
+                 # FP64 pipe itself is busier (comparisons, conversions, division/log/exp sequences)
+                 "roofline": {"bound": "fp64_pipe",
+                              "achieved": FLOPS_PER_PATH_STEP * steps_tot / (t64 / steps64) / 1e12,
+                              "peak": peak_fp64, "unit": "TFLOP/s",
+                              "frac": FLOPS_PER_PATH_STEP * steps_tot / (t64 / steps64) / 1e12 / peak_fp64,
+                              "fp64_pipe_busy_ncu": FP64_PIPE_BUSY_NCU,
+                              "peak_source": "152 SM x 2 DFMA x 2 x sm_max_mhz of MEASURED_PEAKS.json (the "
+                                             "DFMA peak ncu reports; the file measures no FP64 peak)"}},
         "fp32_over_fp64": (t64 / steps64) / per_step,
         "equal_error": {"price_fp32_minus_fp64_in_stderr": price_err_se,
                         "max_risk_fp32_minus_fp64_in_stderr": risk_err_se,

@@ -242,6 +242,14 @@ class Engine:
         _check(lib().cf_value(self._h, modelId.encode(), productId.encode(), ctypes.byref(nc), _p(v), _p(e)))
         return dict(identifiers=self.payoffLabels(productId), values=v, stderrs=e)
 
+    def simulatePaths(self, modelId, productId, num):
+        """mcSimul (mcBase.h:267-308): every path's payoffs, [numPath][nPay]."""
+        npay, _, _ = self.shapes(modelId, productId)
+        out = np.zeros(num.numPath * npay)
+        nc = num.c()
+        _check(lib().cf_simulate_paths(self._h, modelId.encode(), productId.encode(), ctypes.byref(nc), _p(out)))
+        return out.reshape(num.numPath, npay)
+
     def AADriskOne(self, modelId, productId, num, riskPayoff=""):
         npay, npar, _ = self.shapes(modelId, productId)
         v, r = np.zeros(npay), np.zeros(npar)

@@ -152,6 +152,8 @@ struct McParams
     // outputs
     long long* acc;       // [nAcc][2]
     int* err;
+    double* pathOut;      // value launches of mc_kernel: every path's payoffs [path][nPay] (path
+                          // index within the launch), or null
 
     // per-thread scratch of the reverse sweep, layout [field][step][thread]
     void* scratch;

@@ -25,7 +25,7 @@ namespace cf {
 int launch_sobol_points(const unsigned* dir, int dim, long long first, int n, unsigned* out, void* stream);
 int launch_mrg_state(const unsigned long long* A, const unsigned long long* B, unsigned s1, unsigned s2,
                      unsigned long long skip, unsigned* out, void* stream);
-int launch_gauss(int sobol, const unsigned* dir, const unsigned long long* A, const unsigned long long* B,
+int launch_gauss(int sobol, int uniform, const unsigned* dir, const unsigned long long* A, const unsigned long long* B,
                  unsigned s1, unsigned s2, int dim, long long first, int n, double* out, void* stream);
 
 thread_local std::string g_lastError;
@@ -740,7 +740,7 @@ int Context::getPlan(const std::string& mid, const std::string& pid, Plan*& out)
 // into the slot's pinned buffer are all asynchronous on the slot's stream; slot.done is
 // recorded after them.
 int Context::enqueue(Slot& slot, Plan& plan, const cf_num_param& num, bool risk, const double* weights,
-                     long long firstPath)
+                     long long firstPath, double* pathOut)
 {
     if (num.numPath <= 0) return fail(CF_E_ARG, "numPath must be positive");
     if (firstPath < 0 || firstPath % 64) return fail(CF_E_ARG, "firstPath must be a non-negative multiple of 64");
@@ -761,6 +761,7 @@ int Context::enqueue(Slot& slot, Plan& plan, const cf_num_param& num, bool risk,
     p.invnF = sobol ? invnSobol : invnMrg;
     p.nRisk = risk ? plan.nParam : 0;
     p.nAcc = p.nRisk + 2 * plan.nPay + 2;
+    p.pathOut = risk ? nullptr : pathOut;
     // weights (double and float copies), accumulators and the error flag share one buffer
     const size_t wBytes = ((size_t(plan.nPay) * 12 + 255) & ~size_t(255));
     const size_t accBytes = size_t(p.nAcc) * 16;
@@ -1386,6 +1387,29 @@ int cf_aad_risk_multi(cf_context* ctx, const char* modelId, const char* productI
     return ctx->c.riskMulti(*plan, *num, values, risks);
 }
 
+int cf_simulate_paths(cf_context* ctx, const char* modelId, const char* productId, const cf_num_param* num,
+                      double* payoffs)
+{
+    CF_CTX();
+    if (!num || !payoffs) return fail(CF_E_ARG, "null argument");
+    if (num->numPath <= 0) return fail(CF_E_ARG, "numPath must be positive");
+    Plan* plan;
+    int rc = ctx->c.getPlan(modelId ? modelId : "", productId ? productId : "", plan);
+    if (rc) return rc;
+    if (plan->model == MODEL_MULTI)
+        return fail(CF_E_UNSUPPORTED, "mcSimul: per-path payoffs of the multi-asset model are not supported");
+    Context& c = ctx->c;
+    const size_t bytes = size_t(num->numPath) * size_t(plan->nPay) * 8;
+    if ((rc = c.main.paths.ensure(bytes))) return rc;
+    double* dev = static_cast<double*>(c.main.paths.ptr);
+    if ((rc = c.enqueue(*plan, *num, false, nullptr, dev))) return rc;
+    if ((rc = c.fetch(nullptr, nullptr, nullptr, nullptr))) return rc;
+    CF_CUDA(cudaMemcpyAsync(payoffs, dev, bytes, cudaMemcpyDeviceToHost, c.stream));
+    CF_CUDA(cudaStreamSynchronize(c.stream));
+    c.d2h += bytes;
+    return CF_OK;
+}
+
 int cf_enqueue(cf_context* ctx, const char* modelId, const char* productId, const cf_num_param* num, int risk,
                const double* weights, int* launches)
 {
@@ -1499,24 +1523,79 @@ int cf_mrg_state(cf_context* ctx, unsigned seed1, unsigned seed2, int dim, int64
     return CF_OK;
 }
 
-int cf_gaussians(cf_context* ctx, int useSobol, unsigned seed1, unsigned seed2, int dim, int64_t firstPath, int nPaths,
-                 double* out)
+namespace {
+int rng_draws(cf_context* ctx, int uniform, int useSobol, unsigned seed1, unsigned seed2, int dim, int64_t firstPath,
+              int nPaths, double* out)
 {
-    CF_CTX();
     if (dim < 1 || nPaths < 0 || firstPath < 0 || !out || (useSobol && dim > sobol_max_dim()))
-        return fail(CF_E_ARG, "gaussians: bad argument");
+        return fail(CF_E_ARG, uniform ? "uniforms: bad argument" : "gaussians: bad argument");
     DevBuf d, o;
     int rc;
     std::vector<uint32_t> dirs = useSobol ? sobol_dirs(dim) : std::vector<uint32_t>(1);
     if ((rc = d.ensure(dirs.size() * 4)) || (rc = o.ensure(size_t(nPaths) * dim * 8 + 8))) return rc;
     CF_CUDA(cudaMemcpyAsync(d.ptr, dirs.data(), dirs.size() * 4, cudaMemcpyHostToDevice, ctx->c.stream));
-    rc = launch_gauss(useSobol, (const unsigned*)d.ptr, ctx->c.jumpA, ctx->c.jumpB, seed1, seed2, dim, firstPath,
-                      nPaths, (double*)o.ptr, ctx->c.stream);
-    if (rc) return cuda_fail(cudaError_t(rc), "gaussians");
+    rc = launch_gauss(useSobol, uniform, (const unsigned*)d.ptr, ctx->c.jumpA, ctx->c.jumpB, seed1, seed2, dim,
+                      firstPath, nPaths, (double*)o.ptr, ctx->c.stream);
+    if (rc) return cuda_fail(cudaError_t(rc), uniform ? "uniforms" : "gaussians");
     CF_CUDA(cudaMemcpyAsync(out, o.ptr, size_t(nPaths) * dim * 8, cudaMemcpyDeviceToHost, ctx->c.stream));
     CF_CUDA(cudaStreamSynchronize(ctx->c.stream));
     d.release();
     o.release();
+    return CF_OK;
+}
+}  // namespace
+
+int cf_gaussians(cf_context* ctx, int useSobol, unsigned seed1, unsigned seed2, int dim, int64_t firstPath, int nPaths,
+                 double* out)
+{
+    CF_CTX();
+    return rng_draws(ctx, 0, useSobol, seed1, seed2, dim, firstPath, nPaths, out);
+}
+
+int cf_uniforms(cf_context* ctx, int useSobol, unsigned seed1, unsigned seed2, int dim, int64_t firstPath, int nPaths,
+                double* out)
+{
+    CF_CTX();
+    return rng_draws(ctx, 1, useSobol, seed1, seed2, dim, firstPath, nPaths, out);
+}
+
+int cf_model_sim_dim(cf_context* ctx, const char* modelId, const double* productTimeline, int n, int* simDim)
+{
+    CF_CTX();
+    if (!modelId || !simDim || n < 1 || !productTimeline) return fail(CF_E_ARG, "simDim: bad argument");
+    const auto it = ctx->c.models.find(modelId);
+    if (it == ctx->c.models.end()) return fail(CF_E_NOTFOUND, "simDim: model not found");
+    const ModelDesc& m = it->second;
+    const std::vector<double> tl(productTimeline, productTimeline + n);
+    if (m.kind == MODEL_BS)  // mcMdlBS.h:149-195, 280-283: one step per product date after today
+        *simDim = int(std::count_if(tl.begin(), tl.end(), [](double t) { return t > 0.0; }));
+    else if (m.kind == MODEL_DUPIRE)  // mcMdlDupire.h:165-193, 220-223: the refined timeline's steps
+        *simDim = int(fill_data(tl, m.maxDt, kHalfDay, {0.0}).size()) - 1;
+    else
+        return fail(CF_E_UNSUPPORTED, "simDim: multi-asset models take their dimension from a product");
+    return CF_OK;
+}
+
+int cf_product_events(cf_context* ctx, const char* productId, double* times, int* needNumeraire, double* forwardMats,
+                      double* discountMats, double* liborEnds, int capacity, int* count)
+{
+    CF_CTX();
+    if (!productId || !count) return fail(CF_E_ARG, "product events: null argument");
+    const auto it = ctx->c.products.find(productId);
+    if (it == ctx->c.products.end()) return fail(CF_E_NOTFOUND, "product events: product not found");
+    const ProductDesc& pd = it->second;
+    const int n = int(pd.timeline.size());
+    *count = n;
+    if (!times) return CF_OK;
+    if (capacity < n) return fail(CF_E_SHAPE, "product events: capacity too small");
+    for (int e = 0; e < n; ++e)
+    {
+        times[e] = pd.timeline[e];
+        if (needNumeraire) needNumeraire[e] = pd.needNum[e];
+        if (forwardMats) forwardMats[e] = e < int(pd.fwdMat.size()) ? pd.fwdMat[e] : NAN;
+        if (discountMats) discountMats[e] = e < int(pd.discMat.size()) ? pd.discMat[e] : NAN;
+        if (liborEnds) liborEnds[e] = e < int(pd.libEnd.size()) ? pd.libEnd[e] : NAN;
+    }
     return CF_OK;
 }
 

@@ -135,7 +135,7 @@ struct Slot
 {
     cudaStream_t stream = nullptr;
     bool ownsStream = false;
-    DevBuf work, scratch, multiBuf;
+    DevBuf work, scratch, multiBuf, paths;
     PinnedBuf hostAcc, hostW;
     cudaEvent_t done = nullptr;
     McParams last;
@@ -181,8 +181,10 @@ struct Context
     int enqueueMd(Slot& slot, Plan& plan, const cf_num_param& num, bool risk, const double* weights,
                   long long firstPath);
     const ProductDesc* productOf(const Plan& plan) const;
+    // pathOut (value runs of the single-asset kernels): device array receiving every path's
+    // payoffs [path][nPay]
     int enqueue(Slot& slot, Plan& plan, const cf_num_param& num, bool risk, const double* weights,
-                long long firstPath = 0);
+                long long firstPath = 0, double* pathOut = nullptr);
     int fetch(Slot& slot, double* values, double* stderrs, double* aggregate, double* risks);
     bool ready(Slot& slot) const;
     size_t footprint(const Plan& plan, const cf_num_param& num, bool risk) const;
@@ -194,10 +196,10 @@ struct Context
     int finishMulti(Slot& slot, double* values, double* risks);
     int riskMulti(Plan& plan, const cf_num_param& num, double* values, double* risks);
     // main-slot conveniences of the synchronous API
-    int enqueue(Plan& plan, const cf_num_param& num, bool risk, const double* weights)
+    int enqueue(Plan& plan, const cf_num_param& num, bool risk, const double* weights, double* pathOut = nullptr)
     {
         main.stream = stream;
-        return enqueue(main, plan, num, risk, weights);
+        return enqueue(main, plan, num, risk, weights, 0, pathOut);
     }
     int fetch(double* values, double* stderrs, double* aggregate, double* risks)
     {

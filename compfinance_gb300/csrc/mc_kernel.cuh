@@ -232,9 +232,12 @@ __global__ void __launch_bounds__(MC_BLOCK) mc_kernel(const McParams p)
     };
 
     // ---------------------------------------------------------------------------------
-    // One work unit: nAct (0, 1 or 2) paths driven by the Gaussian generator gen(i).
+    // One work unit: nAct (0, 1 or 2) paths driven by the Gaussian generator gen(i); path0 is
+    // the launch-local index of its first path (value launches with p.pathOut write every
+    // path's payoffs there, [path][nPay]).
     // ---------------------------------------------------------------------------------
-    auto runUnit = [&](int nAct, auto&& gen) {
+    auto runUnit = [&](int nAct, long long path0, auto&& gen) {
+        double* const po = RISK ? nullptr : p.pathOut;
         Real x[NP], alive[NP], euro[NP], fE[NP], dE[NP], nE[NP], agg[NP];
         Real cPrev[NP], cPay[NP];  // contingent bond: spot at the previous date, payoff so far
         bool dead[NP];
@@ -316,6 +319,7 @@ __global__ void __launch_bounds__(MC_BLOCK) mc_kernel(const McParams p)
                         fix_add(&paySlab[2 * (payBase + k)], pay);
                         fix_add(&paySlab[2 * (sqBase + k)], pay * pay);
                     }
+                    if (po) po[(path0 + a) * nPay + k] = double(pay);
                     if (RISK) agg[a] += wts[k] * pay;
                 }
             }
@@ -370,6 +374,7 @@ __global__ void __launch_bounds__(MC_BLOCK) mc_kernel(const McParams p)
                 fix_add(&paySlab[2 * payBase], pay);
                 fix_add(&paySlab[2 * sqBase], pay * pay);
                 agg[a] = w0 * pay;
+                if (po) po[(path0 + a) * nPay] = double(pay);
             }
             else if (PROD == PROD_UOC)
             {
@@ -379,12 +384,18 @@ __global__ void __launch_bounds__(MC_BLOCK) mc_kernel(const McParams p)
                 fix_add(&paySlab[2 * (payBase + 1)], euro[a]);
                 fix_add(&paySlab[2 * (sqBase + 1)], euro[a] * euro[a]);
                 agg[a] = w0 * p0 + w1 * euro[a];
+                if (po)
+                {
+                    po[(path0 + a) * nPay] = double(p0);
+                    po[(path0 + a) * nPay + 1] = double(euro[a]);
+                }
             }
             else if (PROD == PROD_CONTINGENT)
             {
                 fix_add(&paySlab[2 * payBase], cPay[a]);
                 fix_add(&paySlab[2 * sqBase], cPay[a] * cPay[a]);
                 agg[a] = w0 * cPay[a];
+                if (po) po[(path0 + a) * nPay] = double(cPay[a]);
             }
             if (RISK)
             {
@@ -625,7 +636,7 @@ __global__ void __launch_bounds__(MC_BLOCK) mc_kernel(const McParams p)
         {
             const long long u = u0 + it;
             const int nAct = u < u1 ? ((2 * u + 1 < p.nPath) ? 2 : 1) : 0;
-            if (ROWACC || nAct) runUnit(nAct, [&](int) { return mrg_gauss<Real>(mrg_next(st)); });
+            if (ROWACC || nAct) runUnit(nAct, 2 * u, [&](int) { return mrg_gauss<Real>(mrg_next(st)); });
             if (ROWACC && (it + 1) % p.nodeFlushUnits == 0) flushNodes();
         }
     }
@@ -652,7 +663,7 @@ __global__ void __launch_bounds__(MC_BLOCK) mc_kernel(const McParams p)
             const long long n = b * 32 + lane;
             const int nAct = (n >= 1 && n <= p.nPath) ? 1 : 0;
             if (ROWACC || nAct)
-                runUnit(nAct, [&](int i) {
+                runUnit(nAct, n - 1, [&](int i) {
                     return sobol_gauss<Real>(base[i] ^ sobol_state(p.sobolDir, nSteps, i, (unsigned long long)lane));
                 });
         }

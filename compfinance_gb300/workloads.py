@@ -190,6 +190,29 @@ def run_multi(grid=(60, 30), paths=1 << 20, reps=1, precision="fp32", device=0):
     return dt
 
 
+def run_superbucket(paths=1 << 20, reps=1, precision="fp32", device=0):
+    """Times `reps` dupireSuperbucket calls of the portfolio (parametric implied surface calibrated
+    to 60x30 local vols, 200 Europeans, 36 monthly steps, Sobol paths, 30x12 risk view) after one
+    warm-up call; returns seconds per call."""
+    import time
+    from compfinance_gb300 import Engine, NumericalParam
+    eng = Engine(device)
+    iv = Engine.ivs("param", 100.0, [SB_IVS["a"], SB_IVS["b"], SB_IVS["c"], SB_IVS["sref"]])
+    isp, mds, itm, mdt = superbucket_grid(60, 30)
+    rk, rm = superbucket_riskview(30, 12)
+    mats, strikes = superbucket_portfolio(10, 20)
+    eng.putEuropeans(mats, strikes, "port")
+    num = NumericalParam(useSobol=True, numPath=int(paths), precision=precision)
+    w = [1.0] * len(mats)
+    eng.dupireSuperbucket(iv, 100.0, 1.0 / 12.0, "port", w, isp, mds, itm, mdt, rk, rm, num)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        eng.dupireSuperbucket(iv, 100.0, 1.0 / 12.0, "port", w, isp, mds, itm, mdt, rk, rm, num)
+    dt = (time.perf_counter() - t0) / max(1, reps)
+    eng.close()
+    return dt
+
+
 # ---------------------------------------------------------------------------------------
 # Multi-asset workload (mcMdlMultiDisplaced.h, mcPrdMulti.h): four correlated assets, one per
 # dynamics of the displacement rule (lognormal, surnormal, subnormal, normal), with dividends;

@@ -129,6 +129,12 @@ int cf_model_grid(cf_context* ctx, const char* modelId, int* nSpots, int* nTimes
 int cf_value(cf_context* ctx, const char* modelId, const char* productId, const cf_num_param* num,
              double* values, double* stderrs);
 
+/* mcSimul, mcBase.h:267-308: the payoffs of every path, payoffs[numPath * nPay] path-major
+ * (path i of the run's random sequence, payoff k in label order), simulated on the device in the
+ * precision of num.  Black-Scholes and Dupire models (CF_E_UNSUPPORTED for the multi-asset one). */
+int cf_simulate_paths(cf_context* ctx, const char* modelId, const char* productId, const cf_num_param* num,
+                      double* payoffs);
+
 /* AADriskOne, main.h:99-173: risks[nParam] of the payoff labelled riskPayoff (NULL or ""
  * = first payoff); payoffValues[nPay]; *riskPayoffValue its value. */
 int cf_aad_risk_one(cf_context* ctx, const char* modelId, const char* productId, const cf_num_param* num,
@@ -231,6 +237,22 @@ int cf_mrg_state(cf_context* ctx, unsigned seed1, unsigned seed2, int dim, int64
 /* Gaussians of paths [firstPath, firstPath+nPaths): out[nPaths*dim] (FP64 form). */
 int cf_gaussians(cf_context* ctx, int useSobol, unsigned seed1, unsigned seed2, int dim, int64_t firstPath,
                  int nPaths, double* out);
+
+/* Uniforms of paths [firstPath, firstPath+nPaths): out[nPaths*dim], what RNG::nextU returns for
+ * them (sobol.h:102-108; mrg32k3a.h:117-148, whose odd paths take 1 - u of the pair's first). */
+int cf_uniforms(cf_context* ctx, int useSobol, unsigned seed1, unsigned seed2, int dim, int64_t firstPath, int nPaths,
+                double* out);
+
+/* ---- model and product shapes (mcBase.h:122-223) ------------------------------------ */
+/* Model::allocate + Model::simDim (mcMdlBS.h:149-195, 280-283; mcMdlDupire.h:165-193, 220-223):
+ * the Gaussians per path of a Black-Scholes or Dupire model of the store simulated on a product
+ * timeline productTimeline[n]. */
+int cf_model_sim_dim(cf_context* ctx, const char* modelId, const double* productTimeline, int n, int* simDim);
+/* Product::timeline / Product::defline (mcBase.h:131-132) of a product of the store: per event
+ * date its time, whether it needs the numeraire, and the maturities of its forward, discount and
+ * libor (which starts at the date); NaN where the date has none.  times == NULL: *count only. */
+int cf_product_events(cf_context* ctx, const char* productId, double* times, int* needNumeraire, double* forwardMats,
+                      double* discountMats, double* liborEnds, int capacity, int* count);
 
 /* ---- device-resident launches (benchmarks and the serving loop) --------------------- */
 /* Enqueues the risk (risk=1, weights[nPay]) or value (risk=0) kernel of (model, product)

@@ -32,10 +32,11 @@ def test_library_exports_every_symbol():
     assert not missing, missing
 
 
-def test_cpp_dropin_header_compiles(tmp_path):
-    src = os.path.join(ROOT, "tests", "cpp", "dropin_main.cpp")
-    r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-I", os.path.join(ROOT, "include"), src],
-                       capture_output=True, text=True)
+@pytest.mark.parametrize("caller", ["dropin_main.cpp", "objects_main.cpp"])
+def test_cpp_dropin_headers_compile(caller):
+    src = os.path.join(ROOT, "tests", "cpp", caller)
+    r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"),
+                        src], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
 
 

@@ -277,6 +277,27 @@ def test_tma_staged_local_vols_bit_identical(eng, monkeypatch, precision):
     assert np.abs(out["1"]["risks"]).max() > 0
 
 
+@pytest.mark.parametrize("case", [("bs", "euro", 1), ("bs_rates", "euro_settle", 0), ("dup20x10", "uoc", 0),
+                                  ("dup20x10", "uoc", 1), ("dup60x30_monthly", "europeans", 1),
+                                  ("bs", "uoc", 0)])
+def test_simulate_paths_vs_oracle(mc_eng, case):
+    """mcSimul's payoff matrix (every path's payoffs, mcBase.h:267-308) against the oracle's
+    per-path payoffs on the same random numbers: FP64 to 1e-12 of the largest payoff, path by
+    path; the path averages equal the valuation entry point's; the FP32 form within FP32
+    rounding of the path arithmetic, path by path."""
+    eng, d = mc_eng
+    mid, pid, sob = case
+    n = 2049  # an odd count: the last antithetic pair has one path
+    got = eng.simulatePaths(mid, pid, num(sob, n))
+    ref = O.paths(O.Model(d["models"][mid]), O.Product(d["products"][pid]), sob, n).reshape(got.shape)
+    assert got.shape == (n, eng.shapes(mid, pid)[0])
+    assert rel_to_max(got, ref) < TOL
+    v = eng.value(mid, pid, num(sob, n))["values"]
+    assert np.abs(got.mean(axis=0) - v).max() <= 1e-13 * np.abs(v).max()
+    g32 = eng.simulatePaths(mid, pid, num(sob, n, "fp32"))
+    assert np.abs(g32 - ref).max() <= 5e-4 * np.abs(ref).max()
+
+
 def test_c2_risk_at_full_size_vs_reference(eng, golden):
     """The 60x30 barrier's AADriskOne at its configured 2^18 mrg32k3a paths against the
     reference's own run (value and all 1801 risks): FP64 to 1e-12; the FP32 form within 0.1

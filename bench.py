@@ -38,6 +38,11 @@ GRID = (60, 30)
 FLOPS_PER_PATH_STEP = 53.0   # algorithmic FP work of value + adjoint per path-step (mrg32k3a)
 TRAFFIC_BYTES_PER_PATH_STEP = 11.72  # measured DRAM traffic of the FP32 risk launch per path-step
 INST_PER_PATH_STEP = 108.2  # measured thread instructions of the FP32 risk launch per path-step
+# serving: slots of the short and long request classes, the path-steps above which a barrier risk
+# is long, stream runs per offered load
+SERVE_SHORT_SLOTS, SERVE_LONG_SLOTS, SERVE_LONG_THRESHOLD = 8, 3, 2e7
+SERVE_LONG_BLOCKS_PER_SM = 4  # resident blocks per SM of a long request: room for short ones
+SERVE_LOAD_RUNS = 5
 # FP64 form (mc_kernel<double>): ncu of the same kernel at 2^18 paths measures its FP64 pipe 82.9%
 # busy; GB300 executes 2 FP64 FMAs per SM per cycle (ncu's peak of the DFMA counter)
 FP64_PIPE_BUSY_NCU = 0.829
@@ -186,8 +191,11 @@ def cpu_multi_asset(seconds=4.0):
 def serving_leg(eng, n, seed):
     """Mixed request stream (seeded Poisson arrivals at 2,000 req/s; 40% BS values, 40% Dupire
     barrier risks of 2^16-2^20 paths on 20x10..120x60 grids with 12..520 steps, 20% European
-    portfolio AADriskMulti), FP32 path form, 64 GB admission budget, 8 slots; then the same
-    requests all submitted at once (the server's batch throughput) and one at a time through the
+    portfolio AADriskMulti), FP32 path form, 64 GB admission budget, 3 runs.  The server runs 8
+    slots for short requests on high-priority streams (values, portfolio risks, barrier risks of
+    at most 2e7 path-steps) and 3 for long risks at low priority with at most 4 resident blocks
+    per SM; then the same requests all submitted at once (the server's batch throughput), at
+    arrival rates offering 80% and 90% of it (5 runs each), and one at a time through the
     synchronous entry points."""
     from compfinance_gb300.api import Server
     from compfinance_gb300.serve_stream import load_store, run_one_at_a_time, run_stream
@@ -199,10 +207,12 @@ def serving_leg(eng, n, seed):
     # one server for every stream below: 8 slots, 64 GB admission budget.  The batch (the same
     # requests all submitted at once: the server's capacity) runs once untimed first, which
     # also grows every slot's device buffers to the stream's sizes, as a long-running server's are.
-    srv = Server(eng, slots=8, hbm_budget=64 << 30)
+    srv = Server(eng, slots=SERVE_SHORT_SLOTS + SERVE_LONG_SLOTS, hbm_budget=64 << 30)
+    srv.configure(SERVE_SHORT_SLOTS, SERVE_LONG_THRESHOLD, 0.0, SERVE_LONG_BLOCKS_PER_SM)
     batch_reqs = [dict(r, t=0.0) for r in stream]
     run_stream(eng, batch_reqs, server=srv)
     stats, makespan, status, _ = run_stream(eng, stream, server=srv)
+    p99_2000 = [stats["p99Ms"]] + [run_stream(eng, stream, server=srv)[0]["p99Ms"] for _ in range(2)]
     bstats, bmakespan, _, _ = run_stream(eng, batch_reqs, server=srv)
     t_seq, steps = run_one_at_a_time(eng, stream)
     served = stats["pathStepsDone"] / makespan
@@ -214,13 +224,24 @@ def serving_leg(eng, n, seed):
     for frac in (0.8, 0.9):
         rate = frac * n / bmakespan
         scaled = [dict(r, t=r["t"] * 2000.0 / rate) for r in stream]
-        lstats, lmakespan, _, _ = run_stream(eng, scaled, server=srv)
-        load.append({"offered_over_batch": frac, "arrival_rate_req_s": rate,
-                     "completed": lstats["completed"], "failed": lstats["failed"],
-                     "p50_ms": lstats["p50Ms"], "p99_ms": lstats["p99Ms"], "mean_ms": lstats["meanMs"],
-                     "makespan_s": lmakespan,
-                     "served_over_batch": lstats["pathStepsDone"] / lmakespan / batch_all})
-    out = {"requests": n, "arrival_rate_req_s": 2000.0, "slots": 8, "hbm_budget_gb": 64,
+        runs = []
+        for _ in range(SERVE_LOAD_RUNS):
+            lstats, lmakespan, _, _ = run_stream(eng, scaled, server=srv)
+            runs.append({"completed": lstats["completed"], "failed": lstats["failed"], "p50_ms": lstats["p50Ms"],
+                         "p99_ms": lstats["p99Ms"], "makespan_s": lmakespan,
+                         "served_over_batch": lstats["pathStepsDone"] / lmakespan / batch_all})
+        p99s = [x["p99_ms"] for x in runs]
+        load.append({"offered_over_batch": frac, "arrival_rate_req_s": rate, "runs": len(runs),
+                     "p99_ms_median": statistics.median(p99s), "p99_ms_max": max(p99s),
+                     "p50_ms_median": statistics.median(x["p50_ms"] for x in runs),
+                     "served_over_batch_min": min(x["served_over_batch"] for x in runs),
+                     "completed_min": min(x["completed"] for x in runs),
+                     "failed_max": max(x["failed"] for x in runs), "p99_ms_runs": p99s})
+    out = {"requests": n, "arrival_rate_req_s": 2000.0,
+           "slots": {"short": SERVE_SHORT_SLOTS, "long": SERVE_LONG_SLOTS,
+                     "long_threshold_path_steps": SERVE_LONG_THRESHOLD,
+                     "long_blocks_per_sm": SERVE_LONG_BLOCKS_PER_SM}, "hbm_budget_gb": 64,
+           "p99_ms_runs_at_2000": p99_2000, "p99_ms_median_at_2000": statistics.median(p99_2000),
             "completed": stats["completed"], "failed": stats["failed"], "rejected": stats["rejected"],
             "p50_ms": stats["p50Ms"], "p99_ms": stats["p99Ms"], "mean_ms": stats["meanMs"],
             "makespan_s": makespan, "served_path_steps_per_s": served,

@@ -503,7 +503,8 @@ class CfServingStats(ctypes.Structure):
                 ("rejected", ctypes.c_uint64), ("cancelled", ctypes.c_uint64), ("timedOut", ctypes.c_uint64),
                 ("p50Ms", ctypes.c_double), ("p99Ms", ctypes.c_double), ("meanMs", ctypes.c_double),
                 ("pathStepsDone", ctypes.c_uint64), ("maxInFlight", ctypes.c_int),
-                ("peakFootprint", ctypes.c_uint64)]
+                ("peakFootprint", ctypes.c_uint64), ("maxStartMs", ctypes.c_double), ("maxStepMs", ctypes.c_double),
+                ("bufferGrowths", ctypes.c_uint64)]
 
 
 STATUS = {0: "queued", 1: "running", 2: "done", 3: "failed", 4: "rejected", 5: "cancelled", 6: "timeout"}
@@ -520,6 +521,13 @@ class Server:
         _check(lib().cf_server_create(engine._h, int(slots), ctypes.c_uint64(hbm_budget), ctypes.byref(h)))
         self._h = h
         self._shape = {}
+
+    def configure(self, short_slots, long_threshold, chunk_path_steps=0.0, long_blocks_per_sm=0):
+        """cf_server_configure: short requests on short_slots high-priority slots, risks above
+        long_threshold path-steps on the others, launched in chunks of chunk_path_steps with at
+        most long_blocks_per_sm resident blocks per SM."""
+        _check(lib().cf_server_configure(self._h, int(short_slots), ctypes.c_double(long_threshold),
+                                         ctypes.c_double(chunk_path_steps), int(long_blocks_per_sm)))
 
     def close(self):
         if self._h:

@@ -46,12 +46,27 @@ int cuda_fail(cudaError_t e, const char* what)
 // ------------------------------------------------------------------------------------
 // Device buffers
 // ------------------------------------------------------------------------------------
-int DevBuf::ensure(size_t n)
+std::atomic<unsigned long long> DevBuf::growths{0};
+
+int DevBuf::ensure(size_t n, cudaStream_t stream)
 {
     if (n <= bytes) return CF_OK;
-    release();
+    ++growths;
     const size_t want = n + n / 4;
-    cudaError_t e = cudaMalloc(&ptr, want);
+    cudaError_t e;
+    if (stream)
+    {
+        // the old buffer is freed after the stream's earlier work, the new one is ready for its later work
+        if (ptr) cudaFreeAsync(ptr, stream);
+        ptr = nullptr;
+        bytes = 0;
+        e = cudaMallocAsync(&ptr, want, stream);
+    }
+    else
+    {
+        release();
+        e = cudaMalloc(&ptr, want);
+    }
     if (e != cudaSuccess)
     {
         ptr = nullptr;
@@ -73,7 +88,9 @@ int PinnedBuf::ensure(size_t n)
 {
     if (n <= bytes) return CF_OK;
     release();
-    const size_t want = n + n / 4;
+    // at least 16 MB (the finished risks of a 200-payoff portfolio on a 120x60 grid are 11.5 MB):
+    // freeing pinned memory waits for the device, so a serving slot should not regrow it
+    const size_t want = std::max(n + n / 4, size_t(16) << 20);
     cudaError_t e = cudaMallocHost(&ptr, want);
     if (e != cudaSuccess)
     {
@@ -678,6 +695,14 @@ int Context::init(int dev)
     CF_CUDA(cudaStreamCreateWithFlags(&ownStream, cudaStreamNonBlocking));
     stream = ownStream;
     CF_CUDA(cudaDeviceGetAttribute(&numSMs, cudaDevAttrMultiProcessorCount, dev));
+    // slot buffers grow through the stream-ordered allocator: the device's pool keeps what they
+    // free for reuse instead of returning it at every synchronisation
+    {
+        cudaMemPool_t pool;
+        uint64_t keep = ~0ULL;
+        if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess)
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
     uint64_t A[64][9], B[64][9];
     mrg_jump_tables(A, B);
     int rc = jump.ensure(sizeof(A) + sizeof(B));
@@ -740,7 +765,7 @@ int Context::getPlan(const std::string& mid, const std::string& pid, Plan*& out)
 // into the slot's pinned buffer are all asynchronous on the slot's stream; slot.done is
 // recorded after them.
 int Context::enqueue(Slot& slot, Plan& plan, const cf_num_param& num, bool risk, const double* weights,
-                     long long firstPath, double* pathOut)
+                     long long firstPath, double* pathOut, long long chunkPaths, int maxBlocksPerSM)
 {
     if (num.numPath <= 0) return fail(CF_E_ARG, "numPath must be positive");
     if (firstPath < 0 || firstPath % 64) return fail(CF_E_ARG, "firstPath must be a non-negative multiple of 64");
@@ -765,7 +790,7 @@ int Context::enqueue(Slot& slot, Plan& plan, const cf_num_param& num, bool risk,
     // weights (double and float copies), accumulators and the error flag share one buffer
     const size_t wBytes = ((size_t(plan.nPay) * 12 + 255) & ~size_t(255));
     const size_t accBytes = size_t(p.nAcc) * 16;
-    int rc = slot.work.ensure(wBytes + accBytes + 256);
+    int rc = slot.work.ensure(wBytes + accBytes + 256, st);
     if (rc) return rc;
     if ((rc = slot.hostAcc.ensure(accBytes + 16))) return rc;
     if ((rc = slot.hostW.ensure(size_t(plan.nPay) * 12 + 16))) return rc;
@@ -827,9 +852,14 @@ int Context::enqueue(Slot& slot, Plan& plan, const cf_num_param& num, bool risk,
     l.smem = stage ? smem1 : smem0;
     const int occ = stage ? occ1 : occ0;
     if (occ < 1) return fail(CF_E_SHAPE, "kernel does not fit on an SM (shared memory " + std::to_string(l.smem) + ")");
+    // chunked runs: the grid and the scratch are sized for one chunk, the launches below cover
+    // the whole run
+    const long long totalPaths = p.nPath;
+    const long long chunk = (!pathOut && chunkPaths >= 64 && chunkPaths < totalPaths) ? (chunkPaths & ~63LL) : totalPaths;
+    p.nPath = chunk;
     const long long threadsNeeded = sobol ? (p.nPath / 32 + 1) * 32 : (p.nPath + 1) / 2;
     long long grid = (threadsNeeded + 127) / 128;
-    const long long maxGrid = (long long)numSMs * occ;
+    const long long maxGrid = (long long)numSMs * (maxBlocksPerSM > 0 ? std::min(occ, maxBlocksPerSM) : occ);
     if (grid > maxGrid) grid = maxGrid;
     if (grid < 1) grid = 1;
     l.grid = int(grid);
@@ -845,11 +875,20 @@ int Context::enqueue(Slot& slot, Plan& plan, const cf_num_param& num, bool risk,
         p.scratchThreads = grid * 128;
         p.scratchFields = mc_scratch_fields(l, mc_rounds(l, p.nPath, grid * 128));
         const size_t bytes = mc_scratch_bytes(l, p, grid);
-        if ((rc = slot.scratch.ensure(bytes))) return rc;
+        if ((rc = slot.scratch.ensure(bytes, st))) return rc;
         p.scratch = slot.scratch.ptr;
     }
-    rc = launch_mc(l, p, st);
-    if (rc) return cuda_fail(cudaError_t(rc), "mc_kernel launch");
+    int nLaunch = 0;
+    for (long long off = 0; off < totalPaths; off += chunk)
+    {
+        McParams q = p;
+        q.firstPath = firstPath + off;
+        q.nPath = std::min(chunk, totalPaths - off);
+        rc = launch_mc(l, q, st);
+        if (rc) return cuda_fail(cudaError_t(rc), "mc_kernel launch");
+        ++nLaunch;
+    }
+    p.nPath = totalPaths;  // the averages are over the whole run
     CF_CUDA(cudaMemcpyAsync(slot.hostAcc.ptr, p.acc, accBytes + 16, cudaMemcpyDeviceToHost, st));
     d2h += accBytes + 16;
     if (!slot.done) CF_CUDA(cudaEventCreateWithFlags(&slot.done, cudaEventDisableTiming));
@@ -859,7 +898,7 @@ int Context::enqueue(Slot& slot, Plan& plan, const cf_num_param& num, bool risk,
     slot.planRef = plan.weak_from_this().lock();
     slot.risk = risk;
     slot.multi = false;
-    slot.launches = 1;
+    slot.launches = nLaunch;
     return CF_OK;
 }
 
@@ -1400,7 +1439,7 @@ int cf_simulate_paths(cf_context* ctx, const char* modelId, const char* productI
         return fail(CF_E_UNSUPPORTED, "mcSimul: per-path payoffs of the multi-asset model are not supported");
     Context& c = ctx->c;
     const size_t bytes = size_t(num->numPath) * size_t(plan->nPay) * 8;
-    if ((rc = c.main.paths.ensure(bytes))) return rc;
+    if ((rc = c.main.paths.ensure(bytes, c.stream))) return rc;
     double* dev = static_cast<double*>(c.main.paths.ptr);
     if ((rc = c.enqueue(*plan, *num, false, nullptr, dev))) return rc;
     if ((rc = c.fetch(nullptr, nullptr, nullptr, nullptr))) return rc;

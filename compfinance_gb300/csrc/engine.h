@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -29,9 +30,13 @@ void results_from_acc(const long long* acc, int nRisk, int nPay, long long nPath
 
 struct DevBuf
 {
+    static std::atomic<unsigned long long> growths;  // allocations made by ensure(), process-wide
     void* ptr = nullptr;
     size_t bytes = 0;
-    int ensure(size_t n);  // grows (never shrinks) the allocation
+    // grows (never shrinks) the allocation; with a stream, through the stream-ordered allocator
+    // on that stream (no device-wide wait: the buffers of serving slots grow while other slots
+    // run)
+    int ensure(size_t n, cudaStream_t stream = nullptr);
     void release();
     DevBuf() = default;
     DevBuf(const DevBuf&) = delete;
@@ -182,9 +187,14 @@ struct Context
                   long long firstPath);
     const ProductDesc* productOf(const Plan& plan) const;
     // pathOut (value runs of the single-asset kernels): device array receiving every path's
-    // payoffs [path][nPay]
+    // payoffs [path][nPay].  chunkPaths > 0 (a multiple of 64): the run is launched as
+    // consecutive path ranges of at most that many paths, each adding into the same exact
+    // accumulators (bit-identical results), so that kernels of other streams get the device
+    // between them.  maxBlocksPerSM > 0 caps the launch's resident blocks per SM below the
+    // kernel's occupancy, leaving room on every SM for kernels of other streams.
     int enqueue(Slot& slot, Plan& plan, const cf_num_param& num, bool risk, const double* weights,
-                long long firstPath = 0, double* pathOut = nullptr);
+                long long firstPath = 0, double* pathOut = nullptr, long long chunkPaths = 0,
+                int maxBlocksPerSM = 0);
     int fetch(Slot& slot, double* values, double* stderrs, double* aggregate, double* risks);
     bool ready(Slot& slot) const;
     size_t footprint(const Plan& plan, const cf_num_param& num, bool risk) const;

@@ -95,7 +95,7 @@ int Context::enqueueMulti(Slot& slot, Plan& plan, const cf_num_param& num, doubl
     const size_t offChunk = offStart + up(size_t(nBuckets + 1) * 4);
     const size_t offRisk = offChunk + up(size_t(nBuckets + 1) * 4);
     const size_t riskBytes = size_t(plan.nParam) * plan.nPay * 8;
-    int rc = slot.multiBuf.ensure(offRisk + up(riskBytes));
+    int rc = slot.multiBuf.ensure(offRisk + up(riskBytes), st);
     if (rc) return rc;
     // the finished risks come back through the pinned buffer, or straight into the caller's
     // array (synchronous calls: a pageable copy, which returns once the data is there)
@@ -151,7 +151,7 @@ int Context::enqueueMulti(Slot& slot, Plan& plan, const cf_num_param& num, doubl
         A.work = reinterpret_cast<int*>(d + offErr + 16);
         const size_t nP = size_t(num.numPath), nE = size_t(nEv);
         const size_t recBytes = up(nP * A.pitch * 8), evBBytes = up(nE * nP * 2), evSBytes = up(nE * nP * 4);
-        if ((rc = slot.scratch.ensure(recBytes + evBBytes + evSBytes + nE * nP * 8))) return rc;
+        if ((rc = slot.scratch.ensure(recBytes + evBBytes + evSBytes + nE * nP * 8, st))) return rc;
         char* sc = static_cast<char*>(slot.scratch.ptr);
         A.rec = reinterpret_cast<unsigned*>(sc);
         A.evB = reinterpret_cast<unsigned short*>(sc + recBytes);
@@ -192,7 +192,7 @@ int Context::enqueueMulti(Slot& slot, Plan& plan, const cf_num_param& num, doubl
         {
             mp.p.scratchThreads = grid * 128;
             mp.p.scratchFields = 1 + 3 * NP;
-            if ((rc = slot.scratch.ensure(size_t(perThread) * mp.p.scratchThreads * (fp32 ? 4 : 8)))) return rc;
+            if ((rc = slot.scratch.ensure(size_t(perThread) * mp.p.scratchThreads * (fp32 ? 4 : 8), st))) return rc;
             mp.p.scratch = slot.scratch.ptr;
         }
         rc = launch_multi(plan.model, sobol, fp32, int(grid), smem, mp, st);

@@ -322,7 +322,7 @@ int Context::enqueueMd(Slot& slot, Plan& plan, const cf_num_param& num, bool ris
     p.nAcc = p.nRisk + 2 * plan.nPay + 2;
     const size_t wBytes = ((size_t(plan.nPay) * 12 + 255) & ~size_t(255));
     const size_t accBytes = size_t(p.nAcc) * 16;
-    int rc = slot.work.ensure(wBytes + accBytes + 256);
+    int rc = slot.work.ensure(wBytes + accBytes + 256, st);
     if (rc) return rc;
     if ((rc = slot.hostAcc.ensure(accBytes + 16))) return rc;
     if ((rc = slot.hostW.ensure(size_t(plan.nPay) * 12 + 16))) return rc;
@@ -352,7 +352,7 @@ int Context::enqueueMd(Slot& slot, Plan& plan, const cf_num_param& num, bool ris
     if (risk)
     {
         const size_t fields = size_t(md_scratch_fields(rng, p));
-        if ((rc = slot.scratch.ensure(fields * size_t(grid) * 128 * (fp32 ? 4 : 8)))) return rc;
+        if ((rc = slot.scratch.ensure(fields * size_t(grid) * 128 * (fp32 ? 4 : 8), st))) return rc;
         p.scratch = slot.scratch.ptr;
     }
     rc = launch_md(rng, fp32, int(grid), smem, p, st);

@@ -3,9 +3,12 @@
 // Requests are admitted in arrival order into a fixed set of execution slots, each with its
 // own CUDA stream, under a device-memory budget: a request starts as soon as a slot is free
 // and its footprint fits the memory left, so work that arrives while other requests are on
-// the GPU overlaps with them.  Finished slots are reaped by polling; queued requests can be
-// cancelled or expire after their queue timeout; a request whose footprint exceeds the whole
-// budget is rejected at submission.  The executor does the work; it is a template parameter
+// the GPU overlaps with them.  Slots and requests may be split into lanes (short and long
+// requests, say): a request takes only slots of its own lane, and arrival order holds within
+// each lane, so a request never waits behind one of another lane.  Finished slots are reaped
+// by polling; queued requests can be cancelled or expire after their queue timeout; a request
+// whose footprint exceeds the whole budget, or whose lane has no slot, is rejected at
+// submission.  The executor does the work; it is a template parameter
 // so that the admission logic is tested on the CPU with a fake executor.
 //
 // Executor interface:
@@ -37,16 +40,24 @@ struct Job
     double queueTimeout = 0;  // seconds a request may wait for a slot (0 = no limit)
     std::string error;
     long long work = 0;       // path-steps, for throughput accounting
+    int lane = 0;             // the slots it may take: those of its lane
 };
 
 template <class Exec>
 class Scheduler
 {
 public:
-    Scheduler(Exec& ex, int nSlots, size_t budget) : ex_(ex), slots_(nSlots, 0), budget_(budget) {}
+    Scheduler(Exec& ex, int nSlots, size_t budget) : ex_(ex), slots_(nSlots, 0), lane_(nSlots, 0), budget_(budget) {}
+
+    // Lane of every slot (one entry per slot; lanes 0..nLanes-1).  Set before the first request.
+    void setLanes(const std::vector<int>& slotLane)
+    {
+        if (slotLane.size() == slots_.size()) lane_ = slotLane;
+    }
+    int slotLane(int s) const { return lane_[s]; }
 
     // Registers a request; a request larger than the whole budget is rejected at once.
-    uint64_t submit(size_t footprint, double queueTimeout, double now, long long work = 0)
+    uint64_t submit(size_t footprint, double queueTimeout, double now, long long work = 0, int lane = 0)
     {
         Job j;
         j.id = ++nextId_;
@@ -54,11 +65,13 @@ public:
         j.tSubmit = now;
         j.queueTimeout = queueTimeout;
         j.work = work;
-        if (footprint > budget_)
+        j.lane = lane;
+        if (footprint > budget_ || std::find(lane_.begin(), lane_.end(), lane) == lane_.end())
         {
             j.status = REJECTED;
-            j.error = "request footprint " + std::to_string(footprint) + " B exceeds the device budget " +
-                      std::to_string(budget_) + " B";
+            j.error = footprint > budget_ ? "request footprint " + std::to_string(footprint) +
+                                                " B exceeds the device budget " + std::to_string(budget_) + " B"
+                                          : "no slot serves lane " + std::to_string(lane);
             j.tDone = now;
             ++rejected_;
         }
@@ -82,8 +95,8 @@ public:
     }
 
     // One scheduling round: reap finished slots, expire queue time-outs, admit in arrival
-    // order while a slot is free and the head request fits the memory left.  Returns the
-    // number of state changes (0 = nothing happened).
+    // order, lane by lane, while a slot of the lane is free and the lane's head request fits the
+    // memory left.  Returns the number of state changes (0 = nothing happened).
     int step(double now)
     {
         int changes = 0;
@@ -127,14 +140,25 @@ public:
             else
                 ++it;
         }
-        while (!queue_.empty())
+        std::vector<char> blocked;  // lanes whose head request waits (arrival order within a lane)
+        for (auto it = queue_.begin(); it != queue_.end();)
         {
-            Job& j = jobs_[queue_.front()];
-            if (inUse_ + j.footprint > budget_) break;  // head of line waits for memory
+            Job& j = jobs_[*it];
+            if (j.lane >= int(blocked.size())) blocked.resize(j.lane + 1, 0);
+            if (blocked[j.lane])
+            {
+                ++it;
+                continue;
+            }
             int s = 0;
-            while (s < int(slots_.size()) && slots_[s]) ++s;
-            if (s == int(slots_.size())) break;
-            queue_.pop_front();
+            while (s < int(slots_.size()) && (slots_[s] || lane_[s] != j.lane)) ++s;
+            if (s == int(slots_.size()) || inUse_ + j.footprint > budget_)  // head of its lane waits
+            {
+                blocked[j.lane] = 1;
+                ++it;
+                continue;
+            }
+            it = queue_.erase(it);
             j.tStart = now;
             const int rc = ex_.start(j, s);
             if (rc)
@@ -207,6 +231,7 @@ public:
 private:
     Exec& ex_;
     std::vector<uint64_t> slots_;
+    std::vector<int> lane_;
     size_t budget_;
     uint64_t nextId_ = 0;
     std::deque<uint64_t> queue_;

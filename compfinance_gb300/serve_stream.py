@@ -1,5 +1,6 @@
 """Drive the serving loop with a timed request stream (workloads.serving_stream) and, for
 comparison, run the same requests one at a time through the synchronous entry points."""
+import gc
 import threading
 import time
 
@@ -53,27 +54,42 @@ def run_stream(eng, stream, slots=8, budget=64 << 30, precision="fp32", keep_res
     if server is not None:
         srv.reset_stats()
     ids = [None] * len(stream)
-    t0 = time.perf_counter()
+    # a collection pause of this process would hold back submissions and release them as a
+    # burst: the client, not the server, would shape the arrivals
+    gc_was = gc.isenabled()
+    gc.disable()
+    try:
+        t0 = time.perf_counter()
 
-    def submitter():
-        for i, r in enumerate(stream):
-            dt = r["t"] - (time.perf_counter() - t0)
-            if dt > 0:
-                time.sleep(dt)
-            ids[i] = srv.submit(r["kind"], r["model"], r["product"], num_of(r, precision))
+        lag = [0.0]
 
-    th = threading.Thread(target=submitter)
-    th.start()
-    th.join()
-    results = {}
-    status = {}
-    for i, rid in enumerate(ids):
-        st = srv.wait(rid)
-        status[i] = st
-        if keep_results and st == "done":
-            results[i] = srv.result(rid)
-    makespan = time.perf_counter() - t0
+        def submitter():
+            for i, r in enumerate(stream):
+                dt = r["t"] - (time.perf_counter() - t0)
+                if dt > 0:
+                    time.sleep(dt)
+                lag[0] = max(lag[0], time.perf_counter() - t0 - r["t"])
+                ids[i] = srv.submit(r["kind"], r["model"], r["product"], num_of(r, precision))
+
+        th = threading.Thread(target=submitter)
+        th.start()
+        th.join()
+        results = {}
+        status = {}
+        for i, rid in enumerate(ids):
+            st = srv.wait(rid)
+            status[i] = st
+            if keep_results and st == "done":
+                results[i] = srv.result(rid)
+            srv.release(rid)  # the server keeps a request's results until they are released
+        makespan = time.perf_counter() - t0
+    finally:
+        if gc_was:
+            gc.enable()
     stats = srv.stats()
+    # how far the submitting thread fell behind the planned arrival times at worst: a late client
+    # releases requests in bursts, which queue
+    stats["submitLagMaxMs"] = 1000.0 * lag[0]
     if server is None:
         srv.close()
     return stats, makespan, status, results

@@ -306,6 +306,9 @@ typedef struct {
     uint64_t pathStepsDone;
     int maxInFlight;
     uint64_t peakFootprint;       /* bytes of admitted requests in flight at once, at most */
+    double maxStartMs;            /* longest host-side start of a request (launch set-up) */
+    double maxStepMs;             /* longest scheduling round of the server thread */
+    uint64_t bufferGrowths;       /* device buffers of the slots grown since the stats were reset */
 } cf_serving_stats;
 
 /* Request status values of cf_server_wait. */
@@ -320,6 +323,16 @@ typedef struct {
 /* A server with `slots` concurrent execution slots (CUDA streams) admitting requests while
  * their device footprint fits hbmBudgetBytes. */
 int cf_server_create(cf_context* ctx, int slots, uint64_t hbmBudgetBytes, cf_server** server);
+/* Serving policy (before the first request): shortSlots of the server's slots, on streams of the
+ * device's highest priority, take only short requests (values, portfolio risks, and risks of at
+ * most longThreshold path-steps); the other slots, at the lowest priority, take only the long
+ * risks, each launched as consecutive path ranges of at most chunkPathSteps path-steps (0: one
+ * launch) with at most longBlocksPerSM resident blocks per SM (0: the kernel's occupancy).  A
+ * risk kernel's blocks stay resident until it ends, so a short request waits for SM room: at
+ * most the running chunk, or none when long kernels leave room.  Arrival order holds within each
+ * class.  Every sum is exact: a request's results do not depend on any of these choices. */
+int cf_server_configure(cf_server* server, int shortSlots, double longThreshold, double chunkPathSteps,
+                        int longBlocksPerSM);
 int cf_server_destroy(cf_server* server);
 int cf_server_submit(cf_server* server, const cf_request* request, uint64_t* id);
 int cf_server_cancel(cf_server* server, uint64_t id);

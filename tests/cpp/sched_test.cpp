@@ -88,6 +88,31 @@ int main()
         s.step(2);
         check(s.completed_ == 1 && s.latencies_.size() == 1 && s.inUse_ == 0, "reset_then_complete");
     }
+    {  // lanes: a short request starts on a short slot while long ones wait for the long slots;
+       // arrival order holds within each lane; a lane with no slot rejects
+        FakeExec ex;
+        Scheduler<FakeExec> s(ex, 3, 1000);
+        s.setLanes({0, 0, 1});  // two short slots, one long slot
+        const uint64_t l1 = s.submit(10, 0, 0, 100, 1), l2 = s.submit(10, 0, 0, 100, 1);
+        const uint64_t s1 = s.submit(1, 0, 0, 1, 0), s2 = s.submit(1, 0, 0, 1, 0), s3 = s.submit(1, 0, 0, 1, 0);
+        ex.duration[l1] = 5.0;
+        s.step(0);
+        check(s.get(l1)->status == RUNNING && s.get(l2)->status == QUEUED, "lane_long_one_slot");
+        check(s.get(s1)->status == RUNNING && s.get(s2)->status == RUNNING && s.get(s3)->status == QUEUED,
+              "lane_short_bypasses_long");
+        check(s.slotLane(s.get(l1)->slot) == 1 && s.slotLane(s.get(s1)->slot) == 0, "lane_slots");
+        ex.now = 1;
+        s.step(1);
+        check(s.get(s3)->status == RUNNING && s.get(l2)->status == QUEUED, "lane_order_within");
+        for (double t = 2; t <= 12; t += 1)
+        {
+            ex.now = t;
+            s.step(t);
+        }
+        check(s.completed_ == 5 && s.get(l2)->tStart >= 5.0, "lane_long_fifo");
+        const uint64_t bad = s.submit(1, 0, 12, 1, 2);
+        check(s.get(bad)->status == REJECTED && !s.get(bad)->error.empty(), "lane_without_slot_rejected");
+    }
     {  // slot-limited admission; small requests overlap
         FakeExec ex;
         Scheduler<FakeExec> s(ex, 3, 1000);

@@ -48,6 +48,34 @@ def test_results_identical_alone_and_in_the_mix(eng):
     assert stats["p99Ms"] >= stats["p50Ms"] > 0
 
 
+def test_lanes_and_chunked_long_requests_identical(eng):
+    """The serving policy of cf_server_configure: short requests on high-priority slots, long risks
+    on low-priority slots, launched as path-range chunks of bounded work.  Every result equals the
+    synchronous call's bit for bit (exact sums over the chunks), in both lanes and both generators;
+    configuring after the first request is refused."""
+    stream = W.serving_stream(n=80, rate=4000.0, seed=23)
+    for r in stream:
+        r["paths"] = min(r["paths"], 1 << 18)
+    stream += [dict(t=0.0, kind="risk", model="dup100_60x30w", product="uoc100_1_1.4_520", paths=(1 << 18) + 4161,
+                    sobol=sob) for sob in (False, True)]
+    srv = Server(eng, slots=6, hbm_budget=64 << 30)
+    srv.configure(short_slots=3, long_threshold=1e7, chunk_path_steps=5e6, long_blocks_per_sm=4)
+    stats, _, status, res = run_stream(eng, stream, keep_results=True, server=srv)
+    assert all(s == "done" for s in status.values()), status
+    longs = 0
+    for i, r in enumerate(stream):
+        v, k = _alone(eng, r)
+        assert np.array_equal(res[i]["values"], v), i
+        if k is not None:
+            assert np.array_equal(res[i]["risks"], k), i
+        if r["kind"] == "risk" and r["paths"] * eng.shapes(r["model"], r["product"])[2] > 1e7:
+            longs += 1
+    assert longs >= 2  # chunked: 5e6 path-steps per launch
+    with pytest.raises(Exception):
+        srv.configure(short_slots=2, long_threshold=1e7)
+    srv.close()
+
+
 def test_admission_budget_rejection_and_failures(eng):
     # A 60x30 barrier risk request at 2^16 FP32 paths runs one unit round and holds ~148 MB of
     # reverse-sweep scratch (7 fields x 157 dates x 2^15 threads x 4 B, plus the blocks' node

@@ -108,17 +108,6 @@ struct MrgState
     unsigned x0, x1, x2, y0, y1, y2;  // x0 newest (reference: myXn, myXn1, myXn2)
 };
 
-// p mod m for any 64-bit p, m = 2^32 - c.
-__host__ __device__ __forceinline__ unsigned mrg_reduce(unsigned long long p, unsigned long long c,
-                                                        unsigned long long m)
-{
-    p = (p >> 32) * c + (p & 0xffffffffULL);
-    p = (p >> 32) * c + (p & 0xffffffffULL);
-    p = (p >> 32) * c + (p & 0xffffffffULL);
-    if (p >= m) p -= m;
-    return (unsigned)p;
-}
-
 // p mod m1 for p < 2^54 with 32-bit multiply-adds: 2^32 = 209 (mod m1).
 __device__ __forceinline__ unsigned mrg_mod1(unsigned long long p)
 {
@@ -146,35 +135,55 @@ __device__ __forceinline__ unsigned mrg_next(MrgState& s)
     return xn > yn ? xn - yn : xn + (unsigned)(MRG_M1 - yn);
 }
 
-__device__ __forceinline__ void mrg_matvec(const unsigned long long* M, unsigned v[3],
-                                           unsigned long long c, unsigned long long m)
+// Jump tables of one generator: record 16k + d (k the position of a hexadecimal digit of the
+// skip, d its value, 1..15) holds M^(d 16^k) mod m, 9 words row-major and 3 words of padding
+// (three 16-byte loads).  A skip of up to 64 bits takes one matrix-vector product per nonzero
+// hexadecimal digit.
+constexpr int MRG_JUMP_RECORD = 12;
+constexpr int MRG_JUMP_RECORDS = 256;
+
+// v <- M v mod m, m = 2^32 - C with C < 2^15 (2^32 = C mod m): each 32 x 32-bit product is
+// folded once and the three of a row summed below 2^49; two more folds leave s < 2^32 + C < 2m
+// and one subtraction the residue.
+template <unsigned C, unsigned M>
+__device__ __forceinline__ void mrg_matvec(const unsigned* rec, unsigned v[3])
 {
+    const uint4* r4 = reinterpret_cast<const uint4*>(rec);
+    const uint4 a = __ldg(r4), b = __ldg(r4 + 1), c = __ldg(r4 + 2);
+    const unsigned e[9] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x};
     unsigned r[3];
+#pragma unroll
     for (int j = 0; j < 3; ++j)
     {
         unsigned long long s = 0;
+#pragma unroll
         for (int l = 0; l < 3; ++l)
         {
-            s += mrg_reduce(M[3 * j + l] * (unsigned long long)v[l], c, m);
-            if (s >= m) s -= m;
+            const unsigned long long q = (unsigned long long)e[3 * j + l] * v[l];
+            s += (unsigned long long)(unsigned)(q >> 32) * C + (unsigned)q;  // < 2^47 + 2^32
         }
-        r[j] = (unsigned)s;
+        s = (unsigned long long)(unsigned)(s >> 32) * C + (unsigned)s;  // < 2^33
+        s = (unsigned long long)(unsigned)(s >> 32) * C + (unsigned)s;  // < 2^32 + C
+        r[j] = unsigned(s >= M ? s - M : s);
     }
     v[0] = r[0]; v[1] = r[1]; v[2] = r[2];
 }
 
-// State after skipping n numbers from the seed state (mrg32k3a.h:306-394 uses binary
-// powers of the recurrence matrices; here the powers A^(2^k) are precomputed tables).
-__device__ __forceinline__ MrgState mrg_jump(unsigned s1, unsigned s2, unsigned long long n,
-                                             const unsigned long long* A, const unsigned long long* B)
+// State after skipping n numbers from the seed state (mrg32k3a.h:306-394 multiplies binary
+// powers of the recurrence matrices; here the powers M^(d 16^k) are precomputed tables).
+__device__ __forceinline__ MrgState mrg_jump(unsigned s1, unsigned s2, unsigned long long n, const unsigned* A,
+                                             const unsigned* B)
 {
     unsigned x[3] = {s1, s1, s1}, y[3] = {s2, s2, s2};
-    for (int k = 0; n; ++k, n >>= 1)
-        if (n & 1)
+    for (int k = 0; n; ++k, n >>= 4)
+    {
+        const int d = int(n & 15);
+        if (d)
         {
-            mrg_matvec(A + 9 * k, x, MRG_C1, MRG_M1);
-            mrg_matvec(B + 9 * k, y, MRG_C2, MRG_M2);
+            mrg_matvec<209u, 4294967087u>(A + (16 * k + d) * MRG_JUMP_RECORD, x);
+            mrg_matvec<22853u, 4294944443u>(B + (16 * k + d) * MRG_JUMP_RECORD, y);
         }
+    }
     return MrgState{x[0], x[1], x[2], y[0], y[1], y[2]};
 }
 

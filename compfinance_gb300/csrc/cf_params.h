@@ -90,8 +90,8 @@ struct McParams
     // random numbers
     unsigned seed1, seed2;
     const unsigned* sobolDir;              // [32][nSteps]
-    const unsigned long long* mrgJumpA;    // [64][9] A^(2^k) mod m1
-    const unsigned long long* mrgJumpB;    // [64][9] B^(2^k) mod m2
+    const unsigned* mrgJumpA;  // jump tables of the first component (mrg_jump)
+    const unsigned* mrgJumpB;  // and of the second
 
     // model: Black-Scholes
     int spotMeasure;
@@ -185,6 +185,11 @@ struct McParams
     // dupire_risk32: local-vol rows staged into shared memory by bulk copies, rowChunk steps per
     // copy, double-buffered (0: rows are read through L1)
     int rowChunk;
+    // dupire_risk32: the launch's round counter (zero at launch), from which blocks claim their
+    // unit rounds, and the most rounds one block may run (0: no limit), set when the scratch
+    // holds fewer than R32_RING round slots
+    unsigned long long* claim;
+    long long roundCap;
 
     // multi-asset displaced model (mcMdlMultiDisplaced.h) with Baskets / Autocall
     // (mcPrdMulti.h); nSteps is the number of time steps, the Gaussians per path nSteps * nA
@@ -222,11 +227,11 @@ int mc_occupancy(const McLaunch& l, size_t smem, int* blocksPerSM);
 // rows staged by bulk copies) that keeps occ0 blocks per SM; sets *smem, returns the occupancy.
 int r32_staging(McLaunch& l, McParams& p, int occ0, size_t* smem);
 // dupire_risk32 keeps the reverse-sweep scratch of its last R32_RING unit rounds (a live path
-// may wait up to two rounds before its sweep); round r uses slot r mod R32_RING, so a launch
-// of fewer rounds needs only as many slots as it has rounds.
+// may wait up to two rounds before its sweep); a block's round r uses slot r mod R32_RING, so a
+// launch of fewer rounds per block (p.roundCap) needs only as many slots.
 constexpr int R32_RING = 3;
-// Unit rounds of a launch of `threads` threads over nPath paths (every thread runs the same
-// number of rounds).
+// Unit rounds of a launch of `threads` threads over nPath paths (the generic kernel's threads
+// all run that many; dupire_risk32's blocks claim rounds as they go, that many on average).
 long long mc_rounds(const McLaunch& l, long long nPath, long long threads);
 // Reverse-sweep scratch fields of a risk launch of `rounds` unit rounds.
 int mc_scratch_fields(const McLaunch& l, long long rounds);

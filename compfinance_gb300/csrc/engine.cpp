@@ -23,9 +23,9 @@
 namespace cf {
 
 int launch_sobol_points(const unsigned* dir, int dim, long long first, int n, unsigned* out, void* stream);
-int launch_mrg_state(const unsigned long long* A, const unsigned long long* B, unsigned s1, unsigned s2,
+int launch_mrg_state(const unsigned* A, const unsigned* B, unsigned s1, unsigned s2,
                      unsigned long long skip, unsigned* out, void* stream);
-int launch_gauss(int sobol, int uniform, const unsigned* dir, const unsigned long long* A, const unsigned long long* B,
+int launch_gauss(int sobol, int uniform, const unsigned* dir, const unsigned* A, const unsigned* B,
                  unsigned s1, unsigned s2, int dim, long long first, int n, double* out, void* stream);
 
 thread_local std::string g_lastError;
@@ -703,14 +703,14 @@ int Context::init(int dev)
         if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess)
             cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
     }
-    uint64_t A[64][9], B[64][9];
+    uint32_t A[256][12], B[256][12];
     mrg_jump_tables(A, B);
     int rc = jump.ensure(sizeof(A) + sizeof(B));
     if (rc) return rc;
     CF_CUDA(cudaMemcpy(jump.ptr, A, sizeof(A), cudaMemcpyHostToDevice));
     CF_CUDA(cudaMemcpy(static_cast<char*>(jump.ptr) + sizeof(A), B, sizeof(B), cudaMemcpyHostToDevice));
-    jumpA = static_cast<const unsigned long long*>(jump.ptr);
-    jumpB = jumpA + 64 * 9;
+    jumpA = static_cast<const unsigned*>(jump.ptr);
+    jumpB = jumpA + 256 * 12;
     // uniforms: mrg32k3a d / (m1 + 1) (mrg32k3a.h:52,78-79), Sobol s * 2.3283064365387e-10 (sobol.h:26)
     std::vector<float> tab(2 * size_t(INVN_PIECES) * 4);
     inv_normal_table(4294967088.0, tab.data());
@@ -787,10 +787,16 @@ int Context::enqueue(Slot& slot, Plan& plan, const cf_num_param& num, bool risk,
     p.nRisk = risk ? plan.nParam : 0;
     p.nAcc = p.nRisk + 2 * plan.nPay + 2;
     p.pathOut = risk ? nullptr : pathOut;
-    // weights (double and float copies), accumulators and the error flag share one buffer
+    // chunked runs (the serving loop's long requests): launches of chunkPaths paths each
+    const long long totalPaths = p.nPath;
+    const long long chunk = (!pathOut && chunkPaths >= 64 && chunkPaths < totalPaths) ? (chunkPaths & ~63LL) : totalPaths;
+    const long long nChunk = (totalPaths + chunk - 1) / chunk;
+    // weights (double and float copies), accumulators, the error flag and one round counter per
+    // launch share one buffer
     const size_t wBytes = ((size_t(plan.nPay) * 12 + 255) & ~size_t(255));
     const size_t accBytes = size_t(p.nAcc) * 16;
-    int rc = slot.work.ensure(wBytes + accBytes + 256, st);
+    const size_t claimBytes = size_t(nChunk) * 8;
+    int rc = slot.work.ensure(wBytes + accBytes + 16 + claimBytes + 256, st);
     if (rc) return rc;
     if ((rc = slot.hostAcc.ensure(accBytes + 16))) return rc;
     if ((rc = slot.hostW.ensure(size_t(plan.nPay) * 12 + 16))) return rc;
@@ -808,7 +814,8 @@ int Context::enqueue(Slot& slot, Plan& plan, const cf_num_param& num, bool risk,
     p.wf = reinterpret_cast<const float*>(wbase + size_t(plan.nPay) * 8);
     p.acc = reinterpret_cast<long long*>(wbase + wBytes);
     p.err = reinterpret_cast<int*>(wbase + wBytes + accBytes);
-    CF_CUDA(cudaMemsetAsync(p.acc, 0, accBytes + 16, st));
+    p.claim = reinterpret_cast<unsigned long long*>(wbase + wBytes + accBytes + 16);
+    CF_CUDA(cudaMemsetAsync(p.acc, 0, accBytes + 16 + claimBytes, st));
 
     McLaunch l{plan.model, plan.prod, sobol ? RNG_SOBOL : RNG_MRG, fp32 ? 1 : 0, risk ? 1 : 0, 0, 0, 0, 0};
     // FP32 Dupire risk runs dupire_risk32 when the plan has its tables and its node slab fits
@@ -854,8 +861,6 @@ int Context::enqueue(Slot& slot, Plan& plan, const cf_num_param& num, bool risk,
     if (occ < 1) return fail(CF_E_SHAPE, "kernel does not fit on an SM (shared memory " + std::to_string(l.smem) + ")");
     // chunked runs: the grid and the scratch are sized for one chunk, the launches below cover
     // the whole run
-    const long long totalPaths = p.nPath;
-    const long long chunk = (!pathOut && chunkPaths >= 64 && chunkPaths < totalPaths) ? (chunkPaths & ~63LL) : totalPaths;
     p.nPath = chunk;
     const long long threadsNeeded = sobol ? (p.nPath / 32 + 1) * 32 : (p.nPath + 1) / 2;
     long long grid = (threadsNeeded + 127) / 128;
@@ -873,7 +878,9 @@ int Context::enqueue(Slot& slot, Plan& plan, const cf_num_param& num, bool risk,
         if (grid * 128 > maxThreads) grid = std::max(1LL, maxThreads / 128);
         l.grid = int(grid);
         p.scratchThreads = grid * 128;
-        p.scratchFields = mc_scratch_fields(l, mc_rounds(l, p.nPath, grid * 128));
+        const long long rounds = mc_rounds(l, p.nPath, grid * 128);
+        p.scratchFields = mc_scratch_fields(l, rounds);
+        p.roundCap = rounds < R32_RING ? rounds : 0;
         const size_t bytes = mc_scratch_bytes(l, p, grid);
         if ((rc = slot.scratch.ensure(bytes, st))) return rc;
         p.scratch = slot.scratch.ptr;
@@ -884,6 +891,7 @@ int Context::enqueue(Slot& slot, Plan& plan, const cf_num_param& num, bool risk,
         McParams q = p;
         q.firstPath = firstPath + off;
         q.nPath = std::min(chunk, totalPaths - off);
+        q.claim = p.claim + nLaunch;
         rc = launch_mc(l, q, st);
         if (rc) return cuda_fail(cudaError_t(rc), "mc_kernel launch");
         ++nLaunch;

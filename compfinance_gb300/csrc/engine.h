@@ -170,8 +170,8 @@ struct Context
     std::map<std::string, ProductDesc> products;
     std::map<std::pair<std::string, std::string>, std::shared_ptr<Plan>> plans;
     DevBuf jump;
-    const unsigned long long* jumpA = nullptr;
-    const unsigned long long* jumpB = nullptr;
+    const unsigned* jumpA = nullptr;
+    const unsigned* jumpB = nullptr;
     DevBuf invn;  // piecewise-cubic inverse normal tables of the FP32 kernels: mrg32k3a, Sobol
     const float* invnMrg = nullptr;
     const float* invnSobol = nullptr;

@@ -109,18 +109,29 @@ static void matmul_mod(const uint64_t a[9], const uint64_t b[9], uint64_t m, uin
     std::copy(t, t + 9, r);
 }
 
-void mrg_jump_tables(uint64_t A[64][9], uint64_t B[64][9])
+void mrg_jump_tables(uint32_t A[256][12], uint32_t B[256][12])
 {
     const uint64_t m1 = 4294967087ULL, m2 = 4294944443ULL;
-    uint64_t a[9] = {0, 1403580, m1 - 810728, 1, 0, 0, 0, 1, 0};
-    uint64_t b[9] = {527612, 0, m2 - 1370589, 1, 0, 0, 0, 1, 0};
-    for (int k = 0; k < 64; ++k)
-    {
-        std::copy(a, a + 9, A[k]);
-        std::copy(b, b + 9, B[k]);
-        matmul_mod(a, a, m1, a);
-        matmul_mod(b, b, m2, b);
-    }
+    const uint64_t a[9] = {0, 1403580, m1 - 810728, 1, 0, 0, 0, 1, 0};
+    const uint64_t b[9] = {527612, 0, m2 - 1370589, 1, 0, 0, 0, 1, 0};
+    auto fill = [](const uint64_t* g, uint64_t m, uint32_t T[256][12]) {
+        uint64_t p[9];  // g^(16^k)
+        std::copy(g, g + 9, p);
+        for (int k = 0; k < 16; ++k)
+        {
+            uint64_t q[9];  // g^(d 16^k)
+            std::copy(p, p + 9, q);
+            std::fill(T[16 * k], T[16 * k] + 12, 0u);
+            for (int d = 1; d < 16; ++d)
+            {
+                for (int i = 0; i < 12; ++i) T[16 * k + d][i] = i < 9 ? uint32_t(q[i]) : 0u;
+                matmul_mod(q, p, m, q);
+            }
+            std::copy(q, q + 9, p);  // g^(16^(k+1))
+        }
+    };
+    fill(a, m1, A);
+    fill(b, m2, B);
 }
 
 double normal_dens(double x) { return x < -10.0 || 10.0 < x ? 0.0 : std::exp(-0.5 * x * x) / 2.506628274631; }

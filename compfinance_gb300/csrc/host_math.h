@@ -29,9 +29,10 @@ std::string fmt2(double x);
 int sobol_max_dim();
 std::vector<uint32_t> sobol_dirs(int dims);
 
-// A^(2^k) mod m1 and B^(2^k) mod m2 for k = 0..63 (row-major 3x3), the matrices of the
-// two mrg32k3a recurrences (mrg32k3a.h:319-358).
-void mrg_jump_tables(uint64_t A[64][9], uint64_t B[64][9]);
+// Jump tables of the two mrg32k3a recurrences (matrices A mod m1 and B mod m2,
+// mrg32k3a.h:319-358): record 16k + d holds A^(d 16^k) (B^(d 16^k)) for k = 0..15 and d = 1..15,
+// row-major 3x3 in words 0..8, words 9..11 and record 16k + 0 zero.
+void mrg_jump_tables(uint32_t A[256][12], uint32_t B[256][12]);
 
 // Beasley-Springer-Moro inverse normal (gaussians.h:47-87), in double.
 double inv_normal_bsm(double p);

@@ -2,8 +2,8 @@
 // smoothed up-and-out payoffs (mcSimulAAD, mcBase.h:427-532, for Dupire, mcMdlDupire.h:238-280,
 // with the products of mcPrd.h:113-288), FP32 path arithmetic, exact fixed-point sums.
 //
-// A block of 128 threads runs work units (an antithetic mrg32k3a pair, or one Sobol path per
-// thread) in three phases:
+// A block of 128 threads runs rounds of work units (an antithetic mrg32k3a pair, or one Sobol
+// path, per thread), claimed from a launch-wide counter, each in three phases:
 //  1. forward: each thread simulates its unit and stores per step one packed word per path
 //     (the interval of the log-spot grid, the interpolation weight t to 22 bits, and whether
 //     the monitoring date at that point fell in the barrier's smoothing band) plus the
@@ -82,8 +82,8 @@ __host__ __device__ inline R32Layout r32_layout(int rng, const McParams& p)
     off += a16(size_t(p.nBucketsF) * 4);
     L.listIdx = off;  // (ring slot << 8) | (thread << 1) | path of the pair
     off += a16(size_t(LIST_CAP) * 2);
-    L.cnt = off;
-    off += 16;
+    L.cnt = off;    // per-warp counts, then the claimed chunk (first round, rounds)
+    off += 32;
     L.mbar = off;   // completion barriers of the two row buffers
     off += 16;
     L.stepc = off;  // per-step node columns and weights of the reverse
@@ -117,6 +117,7 @@ __global__ void __launch_bounds__(RB, (PROD == PROD_UOC && RNGK == RNG_SOBOL) ? 
     int* sBucket = reinterpret_cast<int*>(smem + L.bucket);
     unsigned short* listIdx = reinterpret_cast<unsigned short*>(smem + L.listIdx);
     int* cnt = reinterpret_cast<int*>(smem + L.cnt);
+    long long* sClaim = reinterpret_cast<long long*>(smem + L.cnt + 16);
     unsigned long long* mbar = reinterpret_cast<unsigned long long*>(smem + L.mbar);
     int4* sStepc = reinterpret_cast<int4*>(smem + L.stepc);
     float4* sInvn = reinterpret_cast<float4*>(smem + L.invn);
@@ -568,60 +569,90 @@ __global__ void __launch_bounds__(RB, (PROD == PROD_UOC && RNGK == RNG_SOBOL) ? 
         return k;
     };
 
-    const long long T = (long long)gridDim.x * RB;
-    const long long tg = (long long)blockIdx.x * RB + tid;
+    // Unit rounds (RB units of the generator, or RW Sobol batches of 32 paths) are claimed from
+    // the launch's counter in chunks of G consecutive rounds, G shrinking with the rounds left
+    // (guided self-scheduling): the blocks resident on one SM progress at different speeds, and
+    // with a fixed share each an SM would run its last rounds with few of them left.  A thread
+    // runs the G units of its chunk that follow each other in its generator, with one skip-ahead.
+    // With fewer ring slots than R32_RING a block runs at most p.roundCap rounds (the host's
+    // cap times the grid covers every round).
+    long long it = 0;  // rounds this block has run: round it uses ring slot it mod R32_RING
+    const long long cap = p.roundCap > 0 ? p.roundCap : LLONG_MAX;
+    auto claim = [&](long long nRounds) {  // chunk [sClaim[0], sClaim[0] + sClaim[1]) (uniform)
+        __syncthreads();  // every thread has read the previous chunk
+        if (tid == 0)
+        {
+            const long long seen = (long long)*reinterpret_cast<volatile unsigned long long*>(p.claim);
+            long long g = (nRounds - seen) / (2LL * gridDim.x);
+            g = g > 1 ? g : 1;
+            g = g < cap - it ? g : cap - it;
+            sClaim[1] = g;
+            sClaim[0] = g > 0 ? (long long)atomicAdd(p.claim, (unsigned long long)g) : LLONG_MAX;
+        }
+        __syncthreads();
+    };
     if (RNGK == RNG_MRG)
     {
         const long long nUnits = (p.nPath + 1) / 2;
-        const long long per = (nUnits + T - 1) / T;
-        const long long u0 = tg * per;
-        const long long u1 = u0 + per < nUnits ? u0 + per : nUnits;
-        MrgState st{};
-        if (u0 < u1) st = mrg_jump(p.seed1, p.seed2, (unsigned long long)(p.firstPath / 2 + u0) * nSteps, p.mrgJumpA, p.mrgJumpB);
-        for (long long it = 0; it < per; ++it)  // the same trip count for every thread of the grid
+        const long long nRounds = (nUnits + RB - 1) / RB;
+        for (;;)
         {
-            const long long u = u0 + it;
-            const int nAct = u < u1 ? ((2 * u + 1 < p.nPath) ? 2 : 1) : 0;
-            const int slot = slotOf(it);
-            if (!forward(nAct, [&](int) {
-                    const unsigned d = mrg_next(st);   // in [1, m1]; uniform d / (m1 + 1)
-                    const bool sup = d > 2147483544u;  // (m1 + 1) / 2
-                    return gaussT(sup ? 4294967088u - d : d, sup);
-                }))
-                return;  // a row copy failed (error flag set): the launch fails
-            endRound(slot);
+            claim(nRounds);
+            const long long r0 = sClaim[0], G = sClaim[1];
+            if (r0 >= nRounds) break;
+            const long long u0 = r0 * RB + tid * G;  // this thread's units u0 .. u0 + G - 1
+            MrgState st{};
+            if (u0 < nUnits) st = mrg_jump(p.seed1, p.seed2, (unsigned long long)(p.firstPath / 2 + u0) * nSteps, p.mrgJumpA, p.mrgJumpB);
+            for (long long j = 0; j < G; ++j, ++it)
+            {
+                const long long u = u0 + j;
+                const int nAct = u < nUnits ? ((2 * u + 1 < p.nPath) ? 2 : 1) : 0;
+                const int slot = slotOf(it);
+                if (!forward(nAct, [&](int) {
+                        const unsigned d = mrg_next(st);   // in [1, m1]; uniform d / (m1 + 1)
+                        const bool sup = d > 2147483544u;  // (m1 + 1) / 2
+                        return gaussT(sup ? 4294967088u - d : d, sup);
+                    }))
+                    return;  // a row copy failed (error flag set): the launch fails
+                endRound(slot);
+            }
         }
     }
     else
     {
-        // Sobol: warp w takes batches b = w, w + W, ...; lane l runs index n = 32b + l
+        // Sobol: in round r warp w takes batch b = r RW + w; lane l runs index n = 32b + l
         // (path n-1); state(n) = state(32b) ^ state(l).
         const int pitch = nSteps | 1;
         unsigned* base = reinterpret_cast<unsigned*>(smem + L.base) + wib * pitch;
-        const long long W = T / 32, gw = tg / 32;
         const long long nBatches = p.nPath / 32 + 1;
-        const long long rounds = (nBatches + W - 1) / W;
-        for (long long it = 0; it < rounds; ++it)
+        const long long nRounds = (nBatches + RW - 1) / RW;
+        for (;;)
         {
-            const long long b = gw + it * W;
-            int nAct = 0;
-            if (b < nBatches)
+            claim(nRounds);
+            const long long r0 = sClaim[0], G = sClaim[1];
+            if (r0 >= nRounds) break;
+            for (long long j = 0; j < G; ++j, ++it)
             {
-                __syncwarp();
-                for (int d = lane; d < nSteps; d += 32)
-                    base[d] = sobol_state(p.sobolDir, nSteps, d, (unsigned long long)(p.firstPath + b * 32));
-                __syncwarp();
-                const long long n = b * 32 + lane;
-                nAct = (n >= 1 && n <= p.nPath) ? 1 : 0;
+                const long long b = (r0 + j) * RW + wib;
+                int nAct = 0;
+                if (b < nBatches)
+                {
+                    __syncwarp();
+                    for (int d = lane; d < nSteps; d += 32)
+                        base[d] = sobol_state(p.sobolDir, nSteps, d, (unsigned long long)(p.firstPath + b * 32));
+                    __syncwarp();
+                    const long long n = b * 32 + lane;
+                    nAct = (n >= 1 && n <= p.nPath) ? 1 : 0;
+                }
+                const int slot = slotOf(it);
+                if (!forward(nAct, [&](int i) {
+                        const unsigned sb = base[i] ^ sobol_state(p.sobolDir, nSteps, i, (unsigned long long)lane);
+                        const bool sup = sb >= 2147483648u;
+                        return gaussT(sup ? 0u - sb : (sb > 1u ? sb : 1u), sup);  // state 0 occurs only at index 0
+                    }))
+                    return;  // a row copy failed (error flag set): the launch fails
+                endRound(slot);
             }
-            const int slot = slotOf(it);
-            if (!forward(nAct, [&](int i) {
-                    const unsigned sb = base[i] ^ sobol_state(p.sobolDir, nSteps, i, (unsigned long long)lane);
-                    const bool sup = sb >= 2147483648u;
-                    return gaussT(sup ? 0u - sb : (sb > 1u ? sb : 1u), sup);  // state 0 occurs only at index 0
-                }))
-                return;  // a row copy failed (error flag set): the launch fails
-            endRound(slot);
         }
     }
     endRound(-1);  // the paths still pending after the last round

@@ -172,7 +172,9 @@ extern "C" int cf_aad_risk_aggregate_noalloc(cf_context* ctx, const char* modelI
     const long long threadsNeeded = sobol ? (p.nPath / 32 + 1) * 32 : (p.nPath + 1) / 2;
     long long grid = std::min<long long>((threadsNeeded + 127) / 128, (long long)c.numSMs * occ);
     grid = std::max(1LL, std::min(grid, fitBlocks));
-    p.scratchFields = mc_scratch_fields(l, mc_rounds(l, p.nPath, grid * 128));
+    const long long rounds = mc_rounds(l, p.nPath, grid * 128);
+    p.scratchFields = mc_scratch_fields(l, rounds);
+    p.roundCap = rounds < R32_RING ? rounds : 0;
     if (mc_scratch_bytes(l, p, grid) > CF_NOALLOC_BYTES - offScr)
         return fail_c(CF_E_SHAPE, "noalloc: reverse-sweep scratch exceeds the arena");
     l.grid = int(grid);
@@ -183,6 +185,7 @@ extern "C" int cf_aad_risk_aggregate_noalloc(cf_context* ctx, const char* modelI
     p.wf = reinterpret_cast<const float*>(arena + offW + size_t(plan->nPay) * 8);
     p.acc = reinterpret_cast<long long*>(arena + offAcc);
     p.err = reinterpret_cast<int*>(arena + offAcc + size_t(p.nAcc) * 16);
+    p.claim = reinterpret_cast<unsigned long long*>(arena + offAcc + size_t(p.nAcc) * 16 + 8);  // zeroed with the flag
     double* out = reinterpret_cast<double*>(arena + offOut);
 
     // weights: the caller's doubles are copied in; the FP32 kernel's float copy is made on

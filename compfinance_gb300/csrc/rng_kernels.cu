@@ -15,7 +15,7 @@ __global__ void sobol_points_kernel(const unsigned* dir, int dim, long long firs
     out[i] = sobol_state(dir, dim, d, (unsigned long long)(first + path + 1));
 }
 
-__global__ void mrg_state_kernel(const unsigned long long* A, const unsigned long long* B, unsigned s1, unsigned s2,
+__global__ void mrg_state_kernel(const unsigned* A, const unsigned* B, unsigned s1, unsigned s2,
                                  unsigned long long skip, unsigned* out)
 {
     if (threadIdx.x || blockIdx.x) return;
@@ -26,8 +26,8 @@ __global__ void mrg_state_kernel(const unsigned long long* A, const unsigned lon
 // Gaussians (or, uniform = 1, the uniforms they come from) of paths [first, first+n): Sobol
 // one thread per (path, dim); mrg32k3a one thread per antithetic pair, whose second path takes
 // the negated Gaussians and the uniforms 1 - u (mrg32k3a.h:117-184).
-__global__ void gauss_kernel(int sobol, int uniform, const unsigned* dir, const unsigned long long* A,
-                             const unsigned long long* B, unsigned s1, unsigned s2, int dim, long long first, int n,
+__global__ void gauss_kernel(int sobol, int uniform, const unsigned* dir, const unsigned* A,
+                             const unsigned* B, unsigned s1, unsigned s2, int dim, long long first, int n,
                              double* out)
 {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -61,14 +61,14 @@ int launch_sobol_points(const unsigned* dir, int dim, long long first, int n, un
     return (int)cudaGetLastError();
 }
 
-int launch_mrg_state(const unsigned long long* A, const unsigned long long* B, unsigned s1, unsigned s2,
+int launch_mrg_state(const unsigned* A, const unsigned* B, unsigned s1, unsigned s2,
                      unsigned long long skip, unsigned* out, void* stream)
 {
     mrg_state_kernel<<<1, 32, 0, (cudaStream_t)stream>>>(A, B, s1, s2, skip, out);
     return (int)cudaGetLastError();
 }
 
-int launch_gauss(int sobol, int uniform, const unsigned* dir, const unsigned long long* A, const unsigned long long* B,
+int launch_gauss(int sobol, int uniform, const unsigned* dir, const unsigned* A, const unsigned* B,
                  unsigned s1, unsigned s2, int dim, long long first, int n, double* out, void* stream)
 {
     const long long tot = sobol ? (long long)n * dim : (long long)n / 2 + 2;

@@ -63,7 +63,7 @@ __host__ __device__ inline size_t a16(size_t x) { return (x + 15) & ~size_t(15);
 
 struct R32Layout
 {
-    size_t slab, node, xs, ir, bucket, listIdx, cnt, mbar, stepc, invn, rows, base, total;
+    size_t slab, node, ir, bucket, listIdx, cnt, mbar, stepc, invn, rows, base, total;
 };
 
 __host__ __device__ inline R32Layout r32_layout(int rng, const McParams& p)
@@ -74,12 +74,10 @@ __host__ __device__ inline R32Layout r32_layout(int rng, const McParams& p)
     off += a16(size_t(4 + 2 * p.nPay + 2) * 16);
     L.node = off;  // int32 local-vol node slab of the current chunk
     off += a16(size_t(p.nS) * p.nT * 4);
-    L.xs = off;
-    off += a16(size_t(p.nS + 2) * 4);
     L.ir = off;
     off += a16(size_t(p.nS + 1) * 8);
-    L.bucket = off;
-    off += a16(size_t(p.nBucketsF) * 4);
+    L.bucket = off;  // per bucket: its first knot's interval l0 and the knot above (xs[l0 + 1])
+    off += a16(size_t(p.nBucketsF) * 8);
     L.listIdx = off;  // (ring slot << 8) | (thread << 1) | path of the pair
     off += a16(size_t(LIST_CAP) * 2);
     L.cnt = off;    // per-warp counts, then the claimed chunk (first round, rounds)
@@ -112,9 +110,8 @@ __global__ void __launch_bounds__(RB, (PROD == PROD_UOC && RNGK == RNG_SOBOL) ? 
     long long* slab = reinterpret_cast<long long*>(smem + L.slab);  // [0,2) spot adjoint, payoffs from 8
     long long* paySlab = slab + 8;
     int* node = reinterpret_cast<int*>(smem + L.node);
-    float* sXs = reinterpret_cast<float*>(smem + L.xs);
     float2* sIr = reinterpret_cast<float2*>(smem + L.ir);
-    int* sBucket = reinterpret_cast<int*>(smem + L.bucket);
+    int2* sBucket = reinterpret_cast<int2*>(smem + L.bucket);
     unsigned short* listIdx = reinterpret_cast<unsigned short*>(smem + L.listIdx);
     int* cnt = reinterpret_cast<int*>(smem + L.cnt);
     long long* sClaim = reinterpret_cast<long long*>(smem + L.cnt + 16);
@@ -142,9 +139,12 @@ __global__ void __launch_bounds__(RB, (PROD == PROD_UOC && RNGK == RNG_SOBOL) ? 
         node[i] = 0;
         gnode[i] = 0;
     }
-    for (int i = tid; i < nS + 2; i += RB) sXs[i] = p.xsF[i];
     for (int i = tid; i < nS + 1; i += RB) sIr[i] = make_float2(p.irF[2 * i], p.irF[2 * i + 1]);
-    for (int i = tid; i < p.nBucketsF; i += RB) sBucket[i] = p.bucketF[i];
+    for (int i = tid; i < p.nBucketsF; i += RB)
+    {
+        const int l0 = p.bucketF[i];
+        sBucket[i] = make_int2(l0, __float_as_int(p.xsF[l0 + 1]));
+    }
     const float4* gInvn = reinterpret_cast<const float4*>(p.invnF);
     const bool stageInvn = p.stageY != 0;
     if (stageInvn)
@@ -197,8 +197,8 @@ __global__ void __launch_bounds__(RB, (PROD == PROD_UOC && RNGK == RNG_SOBOL) ? 
     // needs a comparison
     auto search = [&](float xs) -> int {
         const int b = __float2int_rz(fminf(fmaxf((xs - bX0) * bInvW, 0.0f), bMaxF));  // NaN -> 0
-        const int l0 = sBucket[b];
-        const int lo = l0 + (sXs[l0 + 1] <= xs ? 1 : 0);
+        const int2 e = sBucket[b];
+        const int lo = e.x + (__int_as_float(e.y) <= xs ? 1 : 0);
         return lo < nS ? lo : nS;  // +inf would pass the last sentinel
     };
 

@@ -35,7 +35,7 @@ __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(
 // Shared-memory carve-up; identical on host (sizing) and device (pointers).
 struct SmemLayout
 {
-    size_t slab, node, rows, mbar, X, inv, bucket, Y, base, total;
+    size_t slab, node, rows, mbar, claim, X, inv, bucket, Y, base, total;
 };
 
 __host__ __device__ inline SmemLayout mc_layout(int model, int rng, int fp32, int stageY, const McParams& p,
@@ -54,6 +54,8 @@ __host__ __device__ inline SmemLayout mc_layout(int model, int rng, int fp32, in
     L.rows = off;
     if (model == MODEL_DUPIRE && p.nRisk > 0 && fp32) off += align16(size_t(block / 32) * p.nS * 4);
     L.mbar = off;
+    off += 16;
+    L.claim = off;  // the block's claimed chunk of unit rounds (first round, rounds)
     off += 16;
     L.X = L.inv = L.bucket = L.Y = L.base = off;
     if (model == MODEL_DUPIRE)
@@ -623,49 +625,77 @@ __global__ void __launch_bounds__(MC_BLOCK) mc_kernel(const McParams p)
         __syncthreads();
     };
 
+    // Unit rounds (MC_BLOCK units of the generator, or MC_BLOCK / 32 Sobol batches of 32 paths)
+    // are claimed from the launch's counter in chunks of G consecutive rounds, G shrinking with
+    // the rounds left (guided self-scheduling, as in dupire_risk32), so that the blocks of an SM
+    // all run until the work is gone; a thread runs the G units of its chunk that follow each
+    // other in its generator, with one skip-ahead.
+    long long* sClaim = reinterpret_cast<long long*>(smem + L.claim);
+    long long it = 0;  // rounds this block has run (the FP32 node slab is flushed by this count)
+    auto claim = [&](long long nRounds) {  // chunk [sClaim[0], sClaim[0] + sClaim[1]) (uniform)
+        __syncthreads();  // every thread has read the previous chunk
+        if (tid == 0)
+        {
+            const long long seen = (long long)*reinterpret_cast<volatile unsigned long long*>(p.claim);
+            const long long g = (nRounds - seen) / (2LL * gridDim.x);
+            sClaim[1] = g > 1 ? g : 1;
+            sClaim[0] = (long long)atomicAdd(p.claim, (unsigned long long)sClaim[1]);
+        }
+        __syncthreads();
+    };
     if (RNGK == RNG_MRG)
     {
         const long long nUnits = (p.nPath + 1) / 2;
-        const long long per = (nUnits + T - 1) / T;
-        const long long u0 = tg * per;
-        const long long u1 = u0 + per < nUnits ? u0 + per : nUnits;
-        MrgState st{};
-        if (u0 < u1) st = mrg_jump(p.seed1, p.seed2, (unsigned long long)(p.firstPath / 2 + u0) * nSteps, p.mrgJumpA, p.mrgJumpB);
-        // uniform trip count across the block so that the node slab can be flushed in step
-        for (long long it = 0; it < per; ++it)
+        const long long nRounds = (nUnits + MC_BLOCK - 1) / MC_BLOCK;
+        for (;;)
         {
-            const long long u = u0 + it;
-            const int nAct = u < u1 ? ((2 * u + 1 < p.nPath) ? 2 : 1) : 0;
-            if (ROWACC || nAct) runUnit(nAct, 2 * u, [&](int) { return mrg_gauss<Real>(mrg_next(st)); });
-            if (ROWACC && (it + 1) % p.nodeFlushUnits == 0) flushNodes();
+            claim(nRounds);
+            const long long r0 = sClaim[0], G = sClaim[1];
+            if (r0 >= nRounds) break;
+            const long long u0 = r0 * MC_BLOCK + tid * G;  // this thread's units u0 .. u0 + G - 1
+            MrgState st{};
+            if (u0 < nUnits) st = mrg_jump(p.seed1, p.seed2, (unsigned long long)(p.firstPath / 2 + u0) * nSteps, p.mrgJumpA, p.mrgJumpB);
+            for (long long j = 0; j < G; ++j, ++it)
+            {
+                const long long u = u0 + j;
+                const int nAct = u < nUnits ? ((2 * u + 1 < p.nPath) ? 2 : 1) : 0;
+                if (ROWACC || nAct) runUnit(nAct, 2 * u, [&](int) { return mrg_gauss<Real>(mrg_next(st)); });
+                if (ROWACC && (it + 1) % p.nodeFlushUnits == 0) flushNodes();
+            }
         }
     }
     else
     {
-        // Sobol: warp w of the grid takes batches b = w, w + W, ...; lane l runs index
-        // n = 32b + l (path n-1).  state(n) = state(32b) ^ state(l) (gray code is linear
-        // over the disjoint bit ranges of 32b and l).
+        // Sobol: in round r warp w takes batch b = r (MC_BLOCK / 32) + w; lane l runs index
+        // n = 32b + l (path n-1).  state(n) = state(32b) ^ state(l) (gray code is linear over
+        // the disjoint bit ranges of 32b and l).
         const int wib = tid >> 5;
         const int pitch = nSteps | 1;
         unsigned* base = reinterpret_cast<unsigned*>(smem + L.base) + wib * pitch;
-        const long long W = T / 32, gw = tg / 32;
+        constexpr int WB = MC_BLOCK / 32;
         const long long nBatches = p.nPath / 32 + 1;
-        const long long rounds = (nBatches + W - 1) / W;
-        for (long long it = 0; it < rounds; ++it)
+        const long long nRounds = (nBatches + WB - 1) / WB;
+        for (;;)
         {
-            const long long b = gw + it * W;
-            if (ROWACC && it > 0 && it % p.nodeFlushUnits == 0) flushNodes();
-            if (b >= nBatches) continue;
-            __syncwarp();
-            for (int d = lane; d < nSteps; d += 32)
-                base[d] = sobol_state(p.sobolDir, nSteps, d, (unsigned long long)(p.firstPath + b * 32));
-            __syncwarp();
-            const long long n = b * 32 + lane;
-            const int nAct = (n >= 1 && n <= p.nPath) ? 1 : 0;
-            if (ROWACC || nAct)
-                runUnit(nAct, n - 1, [&](int i) {
-                    return sobol_gauss<Real>(base[i] ^ sobol_state(p.sobolDir, nSteps, i, (unsigned long long)lane));
-                });
+            claim(nRounds);
+            const long long r0 = sClaim[0], G = sClaim[1];
+            if (r0 >= nRounds) break;
+            for (long long j = 0; j < G; ++j, ++it)
+            {
+                const long long b = (r0 + j) * WB + wib;
+                if (ROWACC && it > 0 && it % p.nodeFlushUnits == 0) flushNodes();
+                if (b >= nBatches) continue;
+                __syncwarp();
+                for (int d = lane; d < nSteps; d += 32)
+                    base[d] = sobol_state(p.sobolDir, nSteps, d, (unsigned long long)(p.firstPath + b * 32));
+                __syncwarp();
+                const long long n = b * 32 + lane;
+                const int nAct = (n >= 1 && n <= p.nPath) ? 1 : 0;
+                if (ROWACC || nAct)
+                    runUnit(nAct, n - 1, [&](int i) {
+                        return sobol_gauss<Real>(base[i] ^ sobol_state(p.sobolDir, nSteps, i, (unsigned long long)lane));
+                    });
+            }
         }
     }
 

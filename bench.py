@@ -42,6 +42,8 @@ INST_PER_PATH_STEP = 104.6  # measured thread instructions of the FP32 risk laun
 # is long, stream runs per offered load
 SERVE_SHORT_SLOTS, SERVE_LONG_SLOTS, SERVE_LONG_THRESHOLD = 8, 3, 2e7
 SERVE_LONG_BLOCKS_PER_SM = 4  # resident blocks per SM of a long request: room for short ones
+# long risks are admitted least work first (a large one queued longer than this goes first)
+SERVE_LONG_ORDER, SERVE_LONG_AGING_MS = 1, 50.0
 SERVE_LOAD_RUNS = 5
 # FP64 form (mc_kernel<double>): ncu of the same kernel at 2^18 paths measures its FP64 pipe 82.9%
 # busy; GB300 executes 2 FP64 FMAs per SM per cycle (ncu's peak of the DFMA counter)
@@ -194,9 +196,9 @@ def serving_leg(eng, n, seed):
     portfolio AADriskMulti), FP32 path form, 64 GB admission budget, 3 runs.  The server runs 8
     slots for short requests on high-priority streams (values, portfolio risks, barrier risks of
     at most 2e7 path-steps) and 3 for long risks at low priority with at most 4 resident blocks
-    per SM; then the same requests all submitted at once (the server's batch throughput), at
-    arrival rates offering 80% and 90% of it (5 runs each), and one at a time through the
-    synchronous entry points."""
+    per SM, admitted least work first; then the same requests all submitted at once (the server's
+    batch throughput), at arrival rates offering 80%, 85% and 90% of it (5 runs each), and one at a
+    time through the synchronous entry points."""
     from compfinance_gb300.api import Server
     from compfinance_gb300.serve_stream import load_store, run_one_at_a_time, run_stream
     models, products = W.serving_store()
@@ -209,6 +211,7 @@ def serving_leg(eng, n, seed):
     # also grows every slot's device buffers to the stream's sizes, as a long-running server's are.
     srv = Server(eng, slots=SERVE_SHORT_SLOTS + SERVE_LONG_SLOTS, hbm_budget=64 << 30)
     srv.configure(SERVE_SHORT_SLOTS, SERVE_LONG_THRESHOLD, 0.0, SERVE_LONG_BLOCKS_PER_SM)
+    srv.order(1, SERVE_LONG_ORDER, SERVE_LONG_AGING_MS)
     batch_reqs = [dict(r, t=0.0) for r in stream]
     run_stream(eng, batch_reqs, server=srv)
     stats, makespan, status, _ = run_stream(eng, stream, server=srv)
@@ -218,10 +221,10 @@ def serving_leg(eng, n, seed):
     served = stats["pathStepsDone"] / makespan
     batch_all = bstats["pathStepsDone"] / bmakespan
     batch = steps / t_seq
-    # the same requests at arrival rates that offer 80% and 90% of the batch capacity (arrival
-    # times scaled): p99 latency with the server under that load
+    # the same requests at arrival rates that offer 80%, 85% and 90% of the batch capacity
+    # (arrival times scaled): p99 latency with the server under that load
     load = []
-    for frac in (0.8, 0.9):
+    for frac in (0.8, 0.85, 0.9):
         rate = frac * n / bmakespan
         scaled = [dict(r, t=r["t"] * 2000.0 / rate) for r in stream]
         runs = []
@@ -240,7 +243,9 @@ def serving_leg(eng, n, seed):
     out = {"requests": n, "arrival_rate_req_s": 2000.0,
            "slots": {"short": SERVE_SHORT_SLOTS, "long": SERVE_LONG_SLOTS,
                      "long_threshold_path_steps": SERVE_LONG_THRESHOLD,
-                     "long_blocks_per_sm": SERVE_LONG_BLOCKS_PER_SM}, "hbm_budget_gb": 64,
+                     "long_blocks_per_sm": SERVE_LONG_BLOCKS_PER_SM,
+                     "long_order": "least work first" if SERVE_LONG_ORDER else "arrival",
+                     "long_aging_ms": SERVE_LONG_AGING_MS}, "hbm_budget_gb": 64,
            "p99_ms_runs_at_2000": p99_2000, "p99_ms_median_at_2000": statistics.median(p99_2000),
             "completed": stats["completed"], "failed": stats["failed"], "rejected": stats["rejected"],
             "p50_ms": stats["p50Ms"], "p99_ms": stats["p99Ms"], "mean_ms": stats["meanMs"],

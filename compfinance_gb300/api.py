@@ -552,6 +552,11 @@ class Server:
     def cancel(self, rid):
         _check(lib().cf_server_cancel(self._h, ctypes.c_uint64(rid)))
 
+    def order(self, lane, order, aging_ms=0.0):
+        """cf_server_order: admission order of a lane (0 arrival order, 1 least work first, with
+        requests older than aging_ms first)."""
+        _check(lib().cf_server_order(self._h, int(lane), int(order), ctypes.c_double(aging_ms)))
+
     def wait(self, rid, timeout_ms=-1):
         st = ctypes.c_int()
         _check(lib().cf_server_wait(self._h, ctypes.c_uint64(rid), int(timeout_ms), ctypes.byref(st)))

@@ -250,6 +250,16 @@ int cf_server_configure(cf_server* s, int shortSlots, double longThreshold, doub
     return CF_OK;
 }
 
+int cf_server_order(cf_server* s, int lane, int order, double agingMs)
+{
+    if (!s) return fail(CF_E_ARG, "null server");
+    if (lane < 0 || lane > 1 || order < 0 || order > 1 || agingMs < 0)
+        return fail(CF_E_ARG, "server: lane 0 or 1, order 0 or 1, aging >= 0");
+    std::lock_guard<std::mutex> b(s->mu);
+    s->sched.setLaneOrder(lane, order, agingMs * 1e-3);
+    return CF_OK;
+}
+
 int cf_server_destroy(cf_server* s)
 {
     if (!s) return CF_OK;

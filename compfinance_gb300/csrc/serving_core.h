@@ -5,7 +5,9 @@
 // and its footprint fits the memory left, so work that arrives while other requests are on
 // the GPU overlaps with them.  Slots and requests may be split into lanes (short and long
 // requests, say): a request takes only slots of its own lane, and arrival order holds within
-// each lane, so a request never waits behind one of another lane.  Finished slots are reaped
+// each lane, so a request never waits behind one of another lane; a lane may instead admit its
+// least work first (a request that has waited longer than the lane's aging time goes ahead of
+// those, oldest first), so that small requests do not queue behind large ones.  Finished slots are reaped
 // by polling; queued requests can be cancelled or expire after their queue timeout; a request
 // whose footprint exceeds the whole budget, or whose lane has no slot, is rejected at
 // submission.  The executor does the work; it is a template parameter
@@ -23,6 +25,7 @@
 #include <deque>
 #include <map>
 #include <string>
+#include <tuple>
 #include <vector>
 
 namespace cf {
@@ -55,6 +58,21 @@ public:
         if (slotLane.size() == slots_.size()) lane_ = slotLane;
     }
     int slotLane(int s) const { return lane_[s]; }
+
+    // Admission order of a lane: 0 arrival order (the default), 1 least work first, except that
+    // requests older than agingSec go first, in arrival order.
+    void setLaneOrder(int lane, int order, double agingSec)
+    {
+        if (lane < 0) return;
+        if (lane >= int(order_.size()))
+        {
+            order_.resize(lane + 1, 0);
+            aging_.resize(lane + 1, 0.0);
+        }
+        order_[lane] = order;
+        aging_[lane] = agingSec;
+    }
+    int laneOrder(int lane) const { return lane < int(order_.size()) ? order_[lane] : 0; }
 
     // Registers a request; a request larger than the whole budget is rejected at once.
     uint64_t submit(size_t footprint, double queueTimeout, double now, long long work = 0, int lane = 0)
@@ -94,9 +112,9 @@ public:
         return true;
     }
 
-    // One scheduling round: reap finished slots, expire queue time-outs, admit in arrival
-    // order, lane by lane, while a slot of the lane is free and the lane's head request fits the
-    // memory left.  Returns the number of state changes (0 = nothing happened).
+    // One scheduling round: reap finished slots, expire queue time-outs, then admit, lane by
+    // lane in each lane's order, while a slot of the lane is free and the lane's next request fits
+    // the memory left.  Returns the number of state changes (0 = nothing happened).
     int step(double now)
     {
         int changes = 0;
@@ -140,46 +158,44 @@ public:
             else
                 ++it;
         }
-        std::vector<char> blocked;  // lanes whose head request waits (arrival order within a lane)
+        // arrival-order lanes, in one pass over the queue
+        std::vector<char> blocked;  // lanes whose next request waits
         for (auto it = queue_.begin(); it != queue_.end();)
         {
             Job& j = jobs_[*it];
             if (j.lane >= int(blocked.size())) blocked.resize(j.lane + 1, 0);
-            if (blocked[j.lane])
+            if (blocked[j.lane] || laneOrder(j.lane) != 0)
             {
                 ++it;
                 continue;
             }
-            int s = 0;
-            while (s < int(slots_.size()) && (slots_[s] || lane_[s] != j.lane)) ++s;
-            if (s == int(slots_.size()) || inUse_ + j.footprint > budget_)  // head of its lane waits
+            if (!admit(j, now, changes))  // head of its lane waits
             {
                 blocked[j.lane] = 1;
                 ++it;
                 continue;
             }
             it = queue_.erase(it);
-            j.tStart = now;
-            const int rc = ex_.start(j, s);
-            if (rc)
+        }
+        // least-work lanes: aged requests (oldest first), then the least work (then the oldest)
+        for (int lane = 0; lane < int(order_.size()); ++lane)
+        {
+            if (order_[lane] == 0) continue;
+            std::vector<uint64_t> cand;
+            for (uint64_t id : queue_)
+                if (jobs_[id].lane == lane) cand.push_back(id);
+            if (cand.empty()) continue;
+            auto key = [&](uint64_t id) {
+                const Job& j = jobs_[id];
+                const bool aged = aging_[lane] > 0 && now - j.tSubmit > aging_[lane];
+                return std::make_tuple(aged ? 0 : 1, aged ? 0LL : j.work, j.id);  // ids grow with arrival
+            };
+            std::stable_sort(cand.begin(), cand.end(), [&](uint64_t a, uint64_t b) { return key(a) < key(b); });
+            for (uint64_t id : cand)
             {
-                j.status = FAILED;
-                j.error = ex_.error();
-                j.tDone = now;
-                ++failed_;
+                if (!admit(jobs_[id], now, changes)) break;  // the lane's first choice waits
+                queue_.erase(std::find(queue_.begin(), queue_.end(), id));
             }
-            else
-            {
-                j.status = RUNNING;
-                j.slot = s;
-                slots_[s] = j.id;
-                inUse_ += j.footprint;
-                peak_ = std::max(peak_, inUse_);
-                int running = 0;
-                for (uint64_t x : slots_) running += x != 0;
-                maxInFlight_ = std::max(maxInFlight_, running);
-            }
-            ++changes;
         }
         return changes;
     }
@@ -229,9 +245,42 @@ public:
     std::vector<double> latencies_;
 
 private:
+    // Starts j on a free slot of its lane if one is free and its footprint fits; false if it
+    // must wait.  A start that fails ends the job (FAILED) and counts as admitted.
+    bool admit(Job& j, double now, int& changes)
+    {
+        int s = 0;
+        while (s < int(slots_.size()) && (slots_[s] || lane_[s] != j.lane)) ++s;
+        if (s == int(slots_.size()) || inUse_ + j.footprint > budget_) return false;
+        j.tStart = now;
+        const int rc = ex_.start(j, s);
+        if (rc)
+        {
+            j.status = FAILED;
+            j.error = ex_.error();
+            j.tDone = now;
+            ++failed_;
+        }
+        else
+        {
+            j.status = RUNNING;
+            j.slot = s;
+            slots_[s] = j.id;
+            inUse_ += j.footprint;
+            peak_ = std::max(peak_, inUse_);
+            int running = 0;
+            for (uint64_t x : slots_) running += x != 0;
+            maxInFlight_ = std::max(maxInFlight_, running);
+        }
+        ++changes;
+        return true;
+    }
+
     Exec& ex_;
     std::vector<uint64_t> slots_;
     std::vector<int> lane_;
+    std::vector<int> order_;      // per lane: 0 arrival order, 1 least work first
+    std::vector<double> aging_;   // per lane: seconds after which a request goes first
     size_t budget_;
     uint64_t nextId_ = 0;
     std::deque<uint64_t> queue_;

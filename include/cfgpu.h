@@ -333,6 +333,11 @@ int cf_server_create(cf_context* ctx, int slots, uint64_t hbmBudgetBytes, cf_ser
  * class.  Every sum is exact: a request's results do not depend on any of these choices. */
 int cf_server_configure(cf_server* server, int shortSlots, double longThreshold, double chunkPathSteps,
                         int longBlocksPerSM);
+/* Admission order of a lane (0: the short requests, or all of them without cf_server_configure;
+ * 1: the long risks): order 0 is arrival order, order 1 the least work (path-steps) first, where a
+ * request that has waited more than agingMs goes first (oldest first), so that small requests do
+ * not wait behind large ones and none waits indefinitely. */
+int cf_server_order(cf_server* server, int lane, int order, double agingMs);
 int cf_server_destroy(cf_server* server);
 int cf_server_submit(cf_server* server, const cf_request* request, uint64_t* id);
 int cf_server_cancel(cf_server* server, uint64_t id);

@@ -113,6 +113,31 @@ int main()
         const uint64_t bad = s.submit(1, 0, 12, 1, 2);
         check(s.get(bad)->status == REJECTED && !s.get(bad)->error.empty(), "lane_without_slot_rejected");
     }
+    {  // least-work-first lane: the smallest queued long request starts first; one that has waited
+       // past the aging time goes ahead of smaller ones
+        FakeExec ex;
+        Scheduler<FakeExec> s(ex, 2, 1000);
+        s.setLanes({0, 1});
+        s.setLaneOrder(1, 1, 2.5);
+        const uint64_t first = s.submit(1, 0, 0, 50, 1);
+        const uint64_t big = s.submit(1, 0, 0, 400, 1), small = s.submit(1, 0, 0, 100, 1);
+        s.step(0);
+        check(s.get(first)->status == RUNNING && s.get(big)->status == QUEUED, "sjf_first_runs");
+        ex.now = 1;
+        s.step(1);
+        check(s.get(small)->status == RUNNING && s.get(big)->status == QUEUED, "sjf_least_work_next");
+        const uint64_t mid = s.submit(1, 0, 1, 200, 1);
+        ex.now = 3;  // big has waited 3 > 2.5 (aged), mid 2: big goes ahead of the smaller mid
+        s.step(3);
+        check(s.get(big)->status == RUNNING && s.get(mid)->status == QUEUED, "sjf_aged_first");
+        const uint64_t tiny = s.submit(1, 0, 3, 10, 1);
+        s.step(3);
+        check(s.get(tiny)->status == QUEUED, "sjf_slot_busy");
+        s.setLaneOrder(1, 0, 0.0);  // back to arrival order: mid (older) before tiny
+        ex.now = 20;
+        s.step(20);
+        check(s.get(mid)->status == RUNNING && s.get(tiny)->status == QUEUED, "order_back_to_fifo");
+    }
     {  // slot-limited admission; small requests overlap
         FakeExec ex;
         Scheduler<FakeExec> s(ex, 3, 1000);

@@ -51,8 +51,9 @@ def test_results_identical_alone_and_in_the_mix(eng):
 def test_lanes_and_chunked_long_requests_identical(eng):
     """The serving policy of cf_server_configure: short requests on high-priority slots, long risks
     on low-priority slots, launched as path-range chunks of bounded work.  Every result equals the
-    synchronous call's bit for bit (exact sums over the chunks), in both lanes and both generators;
-    configuring after the first request is refused."""
+    synchronous call's bit for bit (exact sums over the chunks), in both lanes and both generators,
+    with the long lane admitting its least work first; configuring after the first request is
+    refused."""
     stream = W.serving_stream(n=80, rate=4000.0, seed=23)
     for r in stream:
         r["paths"] = min(r["paths"], 1 << 18)
@@ -60,6 +61,7 @@ def test_lanes_and_chunked_long_requests_identical(eng):
                     sobol=sob) for sob in (False, True)]
     srv = Server(eng, slots=6, hbm_budget=64 << 30)
     srv.configure(short_slots=3, long_threshold=1e7, chunk_path_steps=5e6, long_blocks_per_sm=4)
+    srv.order(1, 1, 50.0)  # long risks: least work first
     stats, _, status, res = run_stream(eng, stream, keep_results=True, server=srv)
     assert all(s == "done" for s in status.values()), status
     longs = 0

@@ -277,12 +277,16 @@ __global__ void __launch_bounds__(RB, (PROD == PROD_UOC && RNGK == RNG_SOBOL) ? 
 #pragma unroll
             for (int a = 0; a < NP; ++a)
                 if (a < nAct) event(0, a);
-        // steps [s0, s1), with the local-vol entry of interval lo at step s given by row(s, lo)
-        auto steps = [&](int s0, int s1, auto&& row) {
-            for (int s = s0; s < s1; ++s)
+        // steps [s0, s1), with the local-vol row of step s at rowOf(s) (entry lo at rowOf(s)[lo]);
+        // the scratch pointers of the Gaussian and the step words advance by one point per step
+        auto steps = [&](int s0, int s1, auto&& rowOf) {
+            float* pg = fs + F_G * rowStride + s0 * Ti + myCol;
+            unsigned* pw = reinterpret_cast<unsigned*>(fs) + F_W * rowStride + s0 * Ti + myCol;
+            for (int s = s0; s < s1; ++s, pg += Ti, pw += Ti)
             {
                 const float g = gen(s);
-                __stcs(fs + F_G * rowStride + s * Ti + myCol, g);  // streamed: read once, in the reverse
+                __stcs(pg, g);  // streamed: read once, in the reverse
+                const float2* rs = rowOf(s);
 #pragma unroll
                 for (int a = 0; a < NP; ++a)
                 {
@@ -292,10 +296,11 @@ __global__ void __launch_bounds__(RB, (PROD == PROD_UOC && RNGK == RNG_SOBOL) ? 
                     const float2 ir = sIr[lo];
                     const float t2 = fminf((x[a] - ir.x) * ir.y, T_MAX) + 2.0f;
                     const unsigned tq = __float_as_uint(t2) & T_MASK;
-                    const float2 yd = row(s, lo);
+                    float2 yd;
+                    if constexpr (ROWS) yd = rs[lo];  // shared memory
+                    else yd = __ldg(rs + lo);
                     const float v = fmaf(yd.y, t2, yd.x);  // table (y - 2 d, d)
-                    __stcs(reinterpret_cast<unsigned*>(fs) + (F_W + a) * rowStride + s * Ti + myCol,
-                           (unsigned(lo) << LO_SHIFT) | flag[a] | tq);
+                    __stcs(pw + a * rowStride, (unsigned(lo) << LO_SHIFT) | flag[a] | tq);
                     flag[a] = 0;  // the flag of point s + 1 is set by its date, if any
                     x[a] += v * (-0.5f * v + ga);
                 }
@@ -332,12 +337,12 @@ __global__ void __launch_bounds__(RB, (PROD == PROD_UOC && RNGK == RNG_SOBOL) ? 
                 if (tid == 0 && c + 1 < nChunks) issueRows(c + 1);
                 const float2* buf = sRows + b * K * tPitch;  // row s at buf + (s - cK) tPitch
                 const int s0 = c * K;
-                if (nAct) steps(s0, min(s0 + K, nSteps), [&](int s, int lo) { return buf[(s - s0) * tPitch + lo]; });
+                if (nAct) steps(s0, min(s0 + K, nSteps), [&](int s) { return buf + (s - s0) * tPitch; });
             }
         }
         else
         {
-            if (nAct) steps(0, nSteps, [&](int s, int lo) { return __ldg(td + size_t(s) * tPitch + lo); });
+            if (nAct) steps(0, nSteps, [&](int s) { return td + size_t(s) * tPitch; });
         }
         if (!nAct) return true;
 

@@ -109,6 +109,7 @@ class Engine:
         _check(lib().cf_put_black_scholes(self._h, ctypes.c_double(spot), ctypes.c_double(vol), int(bool(qSpot)),
                                           ctypes.c_double(rate), ctypes.c_double(div), id.encode()))
         self._label_cache.pop(("m", id), None)
+        self._label_cache.pop(("mgrid", id), None)
         return id
 
     def putDupire(self, spot, spots, times, vols, maxDt, id):
@@ -118,7 +119,11 @@ class Engine:
             raise CfError(-1, "putDupire: vols must be len(spots) x len(times)")
         _check(lib().cf_put_dupire(self._h, ctypes.c_double(spot), _p(s), len(s), _p(t), len(t), _p(v),
                                    ctypes.c_double(maxDt), id.encode()))
-        self._label_cache.pop(("m", id), None)
+        # a Dupire model's parameter labels depend on its spot and time grid only
+        grid = (s.tobytes(), t.tobytes())
+        if self._label_cache.get(("mgrid", id)) != grid:
+            self._label_cache.pop(("m", id), None)
+            self._label_cache[("mgrid", id)] = grid
         return id
 
     def putEuropean(self, strike, exerciseDate, settlementDate=None, id="european"):
@@ -169,6 +174,7 @@ class Engine:
                                       ctypes.c_double(discRate), _p(rs), len(divDates), _p(dd), _p(dv), _p(co),
                                       ctypes.c_double(lambda_), id.encode()))
         self._label_cache.pop(("m", id), None)
+        self._label_cache.pop(("mgrid", id), None)
         return id
 
     def putBaskets(self, assets, weights, maturity, strikes, id):

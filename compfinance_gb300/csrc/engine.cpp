@@ -453,9 +453,23 @@ int Context::buildPlan(const ModelDesc& m, const ProductDesc& pd, Plan& plan)
         {
             const double sq = std::sqrt(tl[i + 1] - tl[i]);
             sqv[i] = sq;
-            for (int j = 0; j < nS; ++j)
-                Y[size_t(i) * nS + j] = sq * interp_lin(m.times.data(), nT, &m.vols[size_t(j) * nT], tl[i]);
+            // interp_lin of every spot's vols at tl[i], with the time bracket found once per step
             const double* it = std::upper_bound(m.times.data(), m.times.data() + nT, tl[i]);
+            if (it == m.times.data() + nT || it == m.times.data())
+            {
+                const size_t c = it == m.times.data() ? 0 : size_t(nT) - 1;
+                for (int j = 0; j < nS; ++j) Y[size_t(i) * nS + j] = sq * m.vols[size_t(j) * nT + c];
+            }
+            else
+            {
+                const size_t k = size_t(it - m.times.data()) - 1;
+                const double tw = (tl[i] - m.times[k]) / (m.times[k + 1] - m.times[k]);
+                for (int j = 0; j < nS; ++j)
+                {
+                    const double* y = &m.vols[size_t(j) * nT];
+                    Y[size_t(i) * nS + j] = sq * (y[k] + (y[k + 1] - y[k]) * tw);
+                }
+            }
             if (it == m.times.data() + nT || it == m.times.data())
             {
                 colA[i] = colB[i] = it == m.times.data() ? 0 : nT - 1;
@@ -628,7 +642,12 @@ int Context::buildPlan(const ModelDesc& m, const ProductDesc& pd, Plan& plan)
     if (po.empty()) po = {0, 0};
     const size_t oK = pk.vec(kf), oKf = pk.vec(to_f(kf)), oPo = pk.vec(po);
     size_t oDir = 0;
-    if (plan.nSteps <= sobol_max_dim()) oDir = pk.vec(sobol_dirs(plan.nSteps));
+    if (plan.nSteps <= sobol_max_dim())
+    {
+        auto& dirs = sobolDirs[plan.nSteps];  // regenerated once per dimension count
+        if (dirs.empty()) dirs = sobol_dirs(plan.nSteps);
+        oDir = pk.vec(dirs);
+    }
     plan.sobolOk = plan.nSteps <= sobol_max_dim();
 
     int rc = plan.tables.ensure(pk.buf.size());

@@ -170,6 +170,7 @@ struct Context
     std::map<std::string, ProductDesc> products;
     std::map<std::pair<std::string, std::string>, std::shared_ptr<Plan>> plans;
     DevBuf jump;
+    std::map<int, std::vector<uint32_t>> sobolDirs;  // Sobol direction numbers per dimension count
     const unsigned* jumpA = nullptr;
     const unsigned* jumpB = nullptr;
     DevBuf invn;  // piecewise-cubic inverse normal tables of the FP32 kernels: mrg32k3a, Sobol

@@ -380,10 +380,15 @@ __global__ void __launch_bounds__(MD_BLOCK) md_kernel(const McParams p)
     {
         const int pitch = dim | 1;
         unsigned* base = reinterpret_cast<unsigned*>(smem + S.base) + wib * pitch;
-        const long long W = T / 32, gw = tg / 32;
         const long long nB = p.nPath / 32 + 1;
-        for (long long b = gw; b < nB; b += W)
+        for (;;)
         {
+            // warps take batches from the launch counter one at a time: the warps of an SM
+            // progress at different speeds, and a fixed share each would leave the last ones alone
+            unsigned long long bc = 0;
+            if (lane == 0) bc = atomicAdd(p.claim, 1ull);
+            const long long b = (long long)__shfl_sync(0xffffffffu, bc, 0);
+            if (b >= nB) break;
             __syncwarp();
             for (int d = lane; d < dim; d += 32)
                 base[d] = sobol_state(p.sobolDir, dim, d, (unsigned long long)(p.firstPath + b * 32));

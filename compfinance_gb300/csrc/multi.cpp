@@ -87,7 +87,7 @@ int Context::enqueueMulti(Slot& slot, Plan& plan, const cf_num_param& num, doubl
     const size_t accRBytes = size_t(nBuckets) * nParam * 16;
     slot.accVBytes = size_t(nBuckets) * 5 * 16;
     const size_t offAccV = offAccR + up(accRBytes);
-    const size_t offErr = offAccV + up(slot.accVBytes);  // error flag, reverse chunk counter
+    const size_t offErr = offAccV + up(slot.accVBytes);  // error flag, reverse chunk counter, batch counter
     const size_t offCnt = offErr + 256;
     const size_t offCur = offCnt + up(size_t(nBuckets) * 4);
     const size_t zeroEnd = offCur + up(size_t(nBuckets) * 4);
@@ -127,6 +127,7 @@ int Context::enqueueMulti(Slot& slot, Plan& plan, const cf_num_param& num, doubl
     p.mrgJumpA = jumpA;
     p.mrgJumpB = jumpB;
     p.err = reinterpret_cast<int*>(d + offErr);
+    p.claim = reinterpret_cast<unsigned long long*>(d + offErr + 64);  // multi32_forward's Sobol batch counter
     const int* dEvOff = reinterpret_cast<const int*>(d);
     long long* dAccR = reinterpret_cast<long long*>(d + offAccR);
     long long* dAccV = reinterpret_cast<long long*>(d + offAccV);

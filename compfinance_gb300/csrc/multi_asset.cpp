@@ -340,6 +340,7 @@ int Context::enqueueMd(Slot& slot, Plan& plan, const cf_num_param& num, bool ris
     p.wf = reinterpret_cast<const float*>(wbase + size_t(plan.nPay) * 8);
     p.acc = reinterpret_cast<long long*>(wbase + wBytes);
     p.err = reinterpret_cast<int*>(wbase + wBytes + accBytes);
+    p.claim = reinterpret_cast<unsigned long long*>(wbase + wBytes + accBytes + 8);  // zeroed with the flag
     CF_CUDA(cudaMemsetAsync(p.acc, 0, accBytes + 16, st));
 
     const size_t smem = md_smem_bytes(rng, fp32, p);

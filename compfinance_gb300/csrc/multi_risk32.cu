@@ -247,13 +247,18 @@ __global__ void __launch_bounds__(MB) multi32_forward(const Multi32Args A)
     }
     else
     {
-        // warp w takes batches b = w, w + W, ...; lane l runs Sobol index n = 32 b + l (path n - 1)
+        // a warp's batch b: lane l runs Sobol index n = 32 b + l (path n - 1)
         const int pitch = nSteps | 1;
         unsigned* base = reinterpret_cast<unsigned*>(smem + L.base) + wib * pitch;
-        const long long W = T / 32, gw = tg / 32;
         const long long nBatches = nPath / 32 + 1;
-        for (long long b = gw; b < nBatches; b += W)
+        for (;;)
         {
+            // warps take batches from the launch counter one at a time: the warps of an SM
+            // progress at different speeds, and a fixed share each would leave the last ones alone
+            unsigned long long bc = 0;
+            if (lane == 0) bc = atomicAdd(p.claim, 1ull);
+            const long long b = (long long)__shfl_sync(0xffffffffu, bc, 0);
+            if (b >= nBatches) break;
             __syncwarp();
             for (int d = lane; d < nSteps; d += 32)
                 base[d] = sobol_state(p.sobolDir, nSteps, d, (unsigned long long)(p.firstPath + b * 32));

@@ -75,6 +75,25 @@ def test_labels(mc_eng, golden):
         assert dim == len(t["sim_timeline"]) - 1
 
 
+def test_label_cache_follows_the_model(eng):
+    """Parameter labels stay cached while a Dupire model is re-put on the same grid, and follow it
+    when the grid or the model kind changes."""
+    from compfinance_gb300 import workloads as W
+    s, t, v = W.dupire_surface(20, 10)
+    eng.putDupire(W.DUPIRE_SPOT, s, t, v, W.DUPIRE_MAXDT, "lab")
+    first = eng.parameterLabels("lab")
+    assert len(first) == 1 + 20 * 10 and first[0] == "spot"
+    eng.putDupire(W.DUPIRE_SPOT, s, t, v * 1.1, W.DUPIRE_MAXDT, "lab")  # new vols, same grid
+    assert eng.parameterLabels("lab") == first
+    eng.putBlackScholes(100.0, 0.2, 0, 0.0, 0.0, "lab")
+    assert eng.parameterLabels("lab") == ["spot", "vol", "rate", "div"]
+    eng.putDupire(W.DUPIRE_SPOT, s, t, v, W.DUPIRE_MAXDT, "lab")  # back on the first grid
+    assert eng.parameterLabels("lab") == first
+    s2, t2, v2 = W.dupire_surface(12, 6)
+    eng.putDupire(W.DUPIRE_SPOT, s2, t2, v2, W.DUPIRE_MAXDT, "lab")
+    assert len(eng.parameterLabels("lab")) == 1 + 12 * 6
+
+
 def _weights(c, npay):
     w = np.zeros(npay)
     if c["mode"] == "risk":

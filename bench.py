@@ -139,6 +139,14 @@ def _cpu_sample_size(O, m, p, w, threads, seconds):
     return n - n % 2
 
 
+def _host_desc():
+    """The host the CPU legs ran on: architecture, the cores this process may use of those online."""
+    import platform
+    online = os.cpu_count() or 1
+    usable = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else online
+    return f"{platform.machine()}, {usable} usable of {online} online cores"
+
+
 def cpu_baseline(seconds=18.0, threads=None):
     """The oracle's hand-written adjoint (multi-threaded) on a bounded sample of the workload."""
     O, m, p, w = _cpu_case()
@@ -148,7 +156,8 @@ def cpu_baseline(seconds=18.0, threads=None):
     O.risk(m, p, 0, n, w, fast=True, threads=threads)
     dt = time.perf_counter() - t0
     return {"value": n / dt, "unit": "paths/s", "cores": threads, "kind": "port",
-            "sample": f"{n} paths of the same workload (FP64, hand-written adjoint), {dt:.2f} s"}
+            "sample": f"{n} paths of the same workload (FP64, hand-written adjoint), {dt:.2f} s",
+            "host": _host_desc()}
 
 
 def multi_asset_leg(eng, npath=1 << 20):
@@ -380,7 +389,8 @@ def run_reference(args):
     tot = sum(ts)
     value = n * args.steps / tot
     cb = {"value": value, "unit": "paths/s", "cores": threads, "kind": "port",
-          "sample": f"{n} paths per step of the same workload (FP64, hand-written adjoint, {threads} threads)"}
+          "sample": f"{n} paths per step of the same workload (FP64, hand-written adjoint, {threads} threads)",
+          "host": _host_desc()}
     out = {"impl": "reference", "metric": METRIC, "value": value, "unit": "paths/s", "n_gpus": args.gpus,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": tot / args.steps * 1e3,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",

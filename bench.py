@@ -37,7 +37,7 @@ NPATH = 1 << 22
 GRID = (60, 30)
 FLOPS_PER_PATH_STEP = 53.0   # algorithmic FP work of value + adjoint per path-step (mrg32k3a)
 TRAFFIC_BYTES_PER_PATH_STEP = 11.80  # measured DRAM traffic of the FP32 risk launch per path-step
-INST_PER_PATH_STEP = 104.6  # measured thread instructions of the FP32 risk launch per path-step
+INST_PER_PATH_STEP = 99.6  # measured thread instructions of the FP32 risk launch per path-step
 # serving: slots of the short and long request classes, the path-steps above which a barrier risk
 # is long, stream runs per offered load
 SERVE_SHORT_SLOTS, SERVE_LONG_SLOTS, SERVE_LONG_THRESHOLD = 8, 3, 2e7

@@ -247,8 +247,7 @@ int cf_dupire_superbucket(cf_context* ctx, const cf_ivs* ivs, double spot, doubl
     Plan* plan;
     if ((rc = c.getPlan(mid, productId, plan))) return rc;
     std::vector<double> risks(plan->nParam);
-    if ((rc = c.enqueue(*plan, *num, true, notionals))) return rc;
-    if ((rc = c.fetch(nullptr, nullptr, value, risks.data()))) return rc;
+    if ((rc = c.aggregateRisk(*plan, *num, notionals, nullptr, value, risks.data()))) return rc;
     *delta = risks[0];
     const double* micro = risks.data() + 1;
     if (microbucket) std::memcpy(microbucket, micro, size_t(nS) * nT * 8);

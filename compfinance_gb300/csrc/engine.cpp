@@ -985,7 +985,7 @@ int Context::fetch(Slot& slot, double* values, double* stderrs, double* aggregat
 {
     if (!slot.plan) return fail(CF_E_ARG, "nothing enqueued");
     CF_CUDA(cudaEventSynchronize(slot.done));
-    if (slot.multi) return finishMulti(slot, values, risks);
+    if (slot.multi) return finishMulti(slot, values, risks, aggregate);
     const McParams& p = slot.last;
     const long long* acc = static_cast<const long long*>(slot.hostAcc.ptr);
     const int e = *reinterpret_cast<const int*>(acc + 2 * size_t(p.nAcc));
@@ -1438,8 +1438,7 @@ int cf_aad_risk_aggregate(cf_context* ctx, const char* modelId, const char* prod
     Plan* plan;
     int rc = ctx->c.getPlan(modelId ? modelId : "", productId ? productId : "", plan);
     if (rc) return rc;
-    if ((rc = ctx->c.enqueue(*plan, *num, true, notionals))) return rc;
-    return ctx->c.fetch(payoffValues, nullptr, aggregateValue, risks);
+    return ctx->c.aggregateRisk(*plan, *num, notionals, payoffValues, aggregateValue, risks);
 }
 
 int cf_aad_risk_multi(cf_context* ctx, const char* modelId, const char* productId, const cf_num_param* num,

@@ -155,6 +155,7 @@ struct Slot
     std::vector<double> ks;
     int multiParams = 0;
     long long multiPaths = 0;
+    std::vector<double> aggW;  // a multi run's aggregation weights (empty: per-payoff risks)
     size_t accRBytes = 0, accVBytes = 0;
     ~Slot();
 };
@@ -202,9 +203,14 @@ struct Context
     // AADriskMulti: the multi kernel (European portfolios) is asynchronous like enqueue
     bool multiFast(const Plan& plan) const;
     bool multi32Use(const Plan& plan, const cf_num_param& num) const;  // FP32 Dupire: multi_risk32.cu
-    // directRisks: the caller's nParam x nPay array, written before the call returns
-    int enqueueMulti(Slot& slot, Plan& plan, const cf_num_param& num, double* directRisks = nullptr);
-    int finishMulti(Slot& slot, double* values, double* risks);
+    // directRisks: the caller's nParam x nPay array, written before the call returns; aggWeights
+    // (nPay): the run's risks are those of the weighted sum of the payoffs (nParam values)
+    int enqueueMulti(Slot& slot, Plan& plan, const cf_num_param& num, double* directRisks = nullptr,
+                     const double* aggWeights = nullptr);
+    int finishMulti(Slot& slot, double* values, double* risks, double* aggregate = nullptr);
+    // AADriskAggregate on the main slot: values, aggregate and risks of sum_k w_k payoff_k
+    int aggregateRisk(Plan& plan, const cf_num_param& num, const double* weights, double* values, double* aggregate,
+                      double* risks);
     int riskMulti(Plan& plan, const cf_num_param& num, double* values, double* risks);
     // main-slot conveniences of the synchronous API
     int enqueue(Plan& plan, const cf_num_param& num, bool risk, const double* weights, double* pathOut = nullptr)

@@ -30,6 +30,7 @@ struct MultiParams
 size_t multi_smem_bytes(int model, int rng, int fp32, const McParams& p, int nBuckets);
 int multi_occupancy(int model, int rng, int fp32, size_t smem, int* occ);
 int launch_multi(int model, int rng, int fp32, int grid, size_t smem, const MultiParams& mp, void* stream);
+int launch_multi_aggregate(const double* risks, int nParam, int nPay, const double* w, double* out, void* stream);
 int launch_multi_finish(const long long* accR, int nAccParam, int nOut, int nEv, const int* evOff, const double* ks,
                         const int* orig, int nPay, int bs, double n, double* risks, void* stream);
 
@@ -47,7 +48,8 @@ bool Context::multiFast(const Plan& plan) const
     return plan.prod == PROD_EUROPEANS && plan.nEv <= kMultiMaxE && productOf(plan) != nullptr;
 }
 
-int Context::enqueueMulti(Slot& slot, Plan& plan, const cf_num_param& num, double* directRisks)
+int Context::enqueueMulti(Slot& slot, Plan& plan, const cf_num_param& num, double* directRisks,
+                          const double* aggWeights)
 {
     const ProductDesc* pd = productOf(plan);
     if (!multiFast(plan)) return fail(CF_E_UNSUPPORTED, "multi kernel: European portfolios of <= 16 maturities");
@@ -95,14 +97,18 @@ int Context::enqueueMulti(Slot& slot, Plan& plan, const cf_num_param& num, doubl
     const size_t offChunk = offStart + up(size_t(nBuckets + 1) * 4);
     const size_t offRisk = offChunk + up(size_t(nBuckets + 1) * 4);
     const size_t riskBytes = size_t(plan.nParam) * plan.nPay * 8;
-    int rc = slot.multiBuf.ensure(offRisk + up(riskBytes), st);
+    const size_t offW = offRisk + up(riskBytes);  // aggregation weights, then the aggregate's risks
+    const size_t offAgg = offW + up(size_t(plan.nPay) * 8);
+    int rc = slot.multiBuf.ensure(offAgg + up(size_t(plan.nParam) * 8), st);
     if (rc) return rc;
-    // the finished risks come back through the pinned buffer, or straight into the caller's
-    // array (synchronous calls: a pageable copy, which returns once the data is there)
-    slot.accRBytes = directRisks ? 0 : riskBytes;
+    // the finished risks come back through the pinned buffer (all of them, or those of the
+    // weighted aggregate), or straight into the caller's array (synchronous calls: a pageable
+    // copy, which returns once the data is there)
+    slot.aggW.assign(aggWeights ? aggWeights : nullptr, aggWeights ? aggWeights + plan.nPay : nullptr);
+    slot.accRBytes = aggWeights ? size_t(plan.nParam) * 8 : directRisks ? 0 : riskBytes;
     if ((rc = slot.hostAcc.ensure(slot.accRBytes + slot.accVBytes + 16))) return rc;
     const size_t wBytes = slot.evOff.size() * 4 + slot.ks.size() * 12 + slot.orig.size() * 4;
-    if ((rc = slot.hostW.ensure(wBytes + 64))) return rc;
+    if ((rc = slot.hostW.ensure(wBytes + size_t(plan.nPay) * 8 + 64))) return rc;
     char* hw = static_cast<char*>(slot.hostW.ptr);
     char* hKs = hw + slot.evOff.size() * 4;
     char* hKsf = hKs + slot.ks.size() * 8;
@@ -117,6 +123,12 @@ int Context::enqueueMulti(Slot& slot, Plan& plan, const cf_num_param& num, doubl
     if (!e) e = cudaMemcpyAsync(d + offKsf, hKsf, ksf.size() * 4, cudaMemcpyHostToDevice, st);
     if (!e) e = cudaMemcpyAsync(d + offOrig, hOrig, slot.orig.size() * 4, cudaMemcpyHostToDevice, st);
     if (!e) e = cudaMemsetAsync(d + offAccR, 0, zeroEnd - offAccR, st);
+    if (!e && aggWeights)
+    {
+        std::memcpy(hw + wBytes, aggWeights, size_t(plan.nPay) * 8);  // hostW holds wBytes + nPay doubles
+        e = cudaMemcpyAsync(d + offW, hw + wBytes, size_t(plan.nPay) * 8, cudaMemcpyHostToDevice, st);
+        h2d += size_t(plan.nPay) * 8;
+    }
     if (e) return cuda_fail(e, "multi upload");
     h2d += wBytes;
 
@@ -205,16 +217,22 @@ int Context::enqueueMulti(Slot& slot, Plan& plan, const cf_num_param& num, doubl
                              reinterpret_cast<const double*>(d + offKs), reinterpret_cast<const int*>(d + offOrig),
                              plan.nPay, plan.model == MODEL_BS ? 1 : 0, double(num.numPath), dRisk, st);
     if (rc) return cuda_fail(cudaError_t(rc), "multi finish launch");
+    double* dAgg = reinterpret_cast<double*>(d + offAgg);
+    if (aggWeights)
+    {
+        rc = launch_multi_aggregate(dRisk, plan.nParam, plan.nPay, reinterpret_cast<const double*>(d + offW), dAgg, st);
+        if (rc) return cuda_fail(cudaError_t(rc), "multi aggregate launch");
+    }
     char* ha = static_cast<char*>(slot.hostAcc.ptr);
     e = cudaSuccess;
-    if (slot.accRBytes) e = cudaMemcpyAsync(ha, dRisk, slot.accRBytes, cudaMemcpyDeviceToHost, st);
+    if (slot.accRBytes) e = cudaMemcpyAsync(ha, aggWeights ? dAgg : dRisk, slot.accRBytes, cudaMemcpyDeviceToHost, st);
     if (!e) e = cudaMemcpyAsync(ha + slot.accRBytes, dAccV, slot.accVBytes, cudaMemcpyDeviceToHost, st);
     if (!e) e = cudaMemcpyAsync(ha + slot.accRBytes + slot.accVBytes, p.err, 4, cudaMemcpyDeviceToHost, st);
-    if (!e && directRisks) e = cudaMemcpyAsync(directRisks, dRisk, riskBytes, cudaMemcpyDeviceToHost, st);
+    if (!e && directRisks && !aggWeights) e = cudaMemcpyAsync(directRisks, dRisk, riskBytes, cudaMemcpyDeviceToHost, st);
     if (!e && !slot.done) e = cudaEventCreateWithFlags(&slot.done, cudaEventDisableTiming);
     if (!e) e = cudaEventRecord(slot.done, st);
     if (e) return cuda_fail(e, "multi download");
-    d2h += riskBytes + slot.accVBytes + 4;
+    d2h += (aggWeights ? slot.accRBytes : riskBytes) + slot.accVBytes + 4;
     slot.plan = &plan;
     slot.planRef = plan.weak_from_this().lock();
     slot.multi = true;
@@ -233,7 +251,7 @@ bool Context::multi32Use(const Plan& plan, const cf_num_param& num) const
     return !(env && env[0] == '0');
 }
 
-int Context::finishMulti(Slot& slot, double* values, double* risks)
+int Context::finishMulti(Slot& slot, double* values, double* risks, double* aggregate)
 {
     const Plan& plan = *slot.plan;
     const char* ha = static_cast<const char*>(slot.hostAcc.ptr);
@@ -243,6 +261,13 @@ int Context::finishMulti(Slot& slot, double* values, double* risks)
     // risks: finished on the device (multi_finish); values: suffix sums over buckets m > j for
     // each sorted strike j
     if (risks && slot.accRBytes) std::memcpy(risks, ha, slot.accRBytes);
+    const bool agg = aggregate && !slot.aggW.empty();
+    std::vector<double> own;
+    if (!values && agg)
+    {
+        own.resize(plan.nPay);
+        values = own.data();
+    }
     if (!values) return CF_OK;
     const double n = double(slot.multiPaths);
     auto V = [](const long long* a, size_t i) { return fix_value_host(a[2 * i], a[2 * i + 1]); };
@@ -262,7 +287,31 @@ int Context::finishMulti(Slot& slot, double* values, double* risks)
         }
         sorted += nK;
     }
+    if (agg)
+    {
+        double a = 0.0;
+        for (int k = 0; k < plan.nPay; ++k) a += slot.aggW[k] * values[k];
+        *aggregate = a;
+    }
     return CF_OK;
+}
+
+int Context::aggregateRisk(Plan& plan, const cf_num_param& num, const double* weights, double* values,
+                           double* aggregate, double* risks)
+{
+    main.stream = stream;
+    // FP32 European portfolios on Dupire: the portfolio kernels (every payoff's risks, then their
+    // weighted sum on the device) take the work in a fraction of the time of one aggregated
+    // adjoint through the generic kernel; the risks are the same linear functional of the paths
+    if (multiFast(plan) && multi32Use(plan, num))
+    {
+        int rc = enqueueMulti(main, plan, num, nullptr, weights);
+        if (rc) return rc;
+        return fetch(main, values, nullptr, aggregate, risks);
+    }
+    int rc = enqueue(main, plan, num, true, weights);
+    if (rc) return rc;
+    return fetch(main, values, nullptr, aggregate, risks);
 }
 
 int Context::riskMulti(Plan& plan, const cf_num_param& num, double* values, double* risks)

@@ -393,6 +393,24 @@ __global__ void multi_finish(const long long* __restrict__ accR, int nAccParam, 
     }
 }
 
+// Risks of a weighted sum of the payoffs: out[j] = sum_k w[k] risks[j][k] (the finished
+// per-payoff risks, [nParam][nPay]); one thread per parameter, payoffs in order.
+__global__ void multi_aggregate_kernel(const double* risks, int nParam, int nPay, const double* w, double* out)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= nParam) return;
+    const double* row = risks + size_t(j) * nPay;
+    double a = 0.0;
+    for (int k = 0; k < nPay; ++k) a += w[k] * row[k];
+    out[j] = a;
+}
+
+int launch_multi_aggregate(const double* risks, int nParam, int nPay, const double* w, double* out, void* stream)
+{
+    multi_aggregate_kernel<<<(nParam + 127) / 128, 128, 0, (cudaStream_t)stream>>>(risks, nParam, nPay, w, out);
+    return (int)cudaGetLastError();
+}
+
 int launch_multi_finish(const long long* accR, int nAccParam, int nOut, int nEv, const int* evOff, const double* ks,
                         const int* orig, int nPay, int bs, double n, double* risks, void* stream)
 {

@@ -30,6 +30,31 @@ def portfolio(eng):
     return m, p
 
 
+@pytest.mark.parametrize("sob", [1, 0])
+def test_aggregate_fp32_through_the_portfolio_kernels(eng, portfolio, monkeypatch, sob):
+    """FP32 AADriskAggregate of a European portfolio on Dupire runs the portfolio kernels and weighs
+    the payoffs' risks on the device: it equals the weighted sum of AADriskMulti's risks on the same
+    paths (to the rounding of the sum), and agrees with the generic kernel's aggregated adjoint
+    (CF_FAST32=0) within 0.1 Monte Carlo standard error of each risk."""
+    n = 1 << 16
+    rs = np.random.RandomState(5)
+    w = rs.uniform(-1.0, 2.0, 200)
+    a = eng.AADriskAggregate("c4dup", "c4port", w, num(sob, n, "fp32"))
+    m = eng.AADriskMulti("c4dup", "c4port", num(sob, n, "fp32"))
+    assert rel_to_max(a["risks"], m["risks"] @ w) < 1e-12
+    assert rel_to_max(np.array([a["riskPayoffValue"]]), np.array([m["values"] @ w])) < 1e-12
+    assert rel_to_max(a["payoffValues"], m["values"]) == 0.0
+    monkeypatch.setenv("CF_FAST32", "0")
+    g = eng.AADriskAggregate("c4dup", "c4port", w, num(sob, n, "fp32"))
+    monkeypatch.delenv("CF_FAST32")
+    # standard error of each risk from 8 independent FP32 runs at a quarter of the paths
+    se = np.std([eng.AADriskAggregate("c4dup", "c4port", w, num(0, n // 4, "fp32", seed1=900 + k, seed2=31 + k))["risks"]
+                 for k in range(8)], axis=0, ddof=1) / 2.0
+    mask = se > 1e-3 * np.abs(g["risks"]).max()
+    assert np.max(np.abs(a["risks"] - g["risks"])[mask] / se[mask]) < 0.1
+    assert abs(a["riskPayoffValue"] - g["riskPayoffValue"]) < 1e-4 * abs(g["riskPayoffValue"])
+
+
 def test_multi_c4_shape_fp64_vs_oracle(eng, portfolio):
     """200 payoffs x 1801 parameters, 36 monthly steps: exact per-payoff path averages."""
     m, p = portfolio

@@ -1426,8 +1426,7 @@ int cf_aad_risk_one(cf_context* ctx, const char* modelId, const char* productId,
     if ((rc = payoff_index(*plan, ctx->c.products[productId], riskPayoff, &k))) return rc;
     std::vector<double> w(plan->nPay, 0.0);
     w[k] = 1.0;
-    if ((rc = ctx->c.enqueue(*plan, *num, true, w.data()))) return rc;
-    return ctx->c.fetch(payoffValues, nullptr, riskPayoffValue, risks);
+    return ctx->c.aggregateRisk(*plan, *num, w.data(), payoffValues, riskPayoffValue, risks);
 }
 
 int cf_aad_risk_aggregate(cf_context* ctx, const char* modelId, const char* productId, const double* notionals,

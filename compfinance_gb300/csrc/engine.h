@@ -208,7 +208,7 @@ struct Context
     int enqueueMulti(Slot& slot, Plan& plan, const cf_num_param& num, double* directRisks = nullptr,
                      const double* aggWeights = nullptr);
     int finishMulti(Slot& slot, double* values, double* risks, double* aggregate = nullptr);
-    // AADriskAggregate on the main slot: values, aggregate and risks of sum_k w_k payoff_k
+    // AADriskOne / AADriskAggregate on the main slot: values, aggregate and risks of sum_k w_k payoff_k
     int aggregateRisk(Plan& plan, const cf_num_param& num, const double* weights, double* values, double* aggregate,
                       double* risks);
     int riskMulti(Plan& plan, const cf_num_param& num, double* values, double* risks);

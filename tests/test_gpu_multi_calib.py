@@ -32,9 +32,9 @@ def portfolio(eng):
 
 @pytest.mark.parametrize("sob", [1, 0])
 def test_aggregate_fp32_through_the_portfolio_kernels(eng, portfolio, monkeypatch, sob):
-    """FP32 AADriskAggregate of a European portfolio on Dupire runs the portfolio kernels and weighs
-    the payoffs' risks on the device: it equals the weighted sum of AADriskMulti's risks on the same
-    paths (to the rounding of the sum), and agrees with the generic kernel's aggregated adjoint
+    """FP32 AADriskAggregate (and AADriskOne) of a European portfolio on Dupire runs the portfolio
+    kernels and weighs the payoffs' risks on the device: it equals the weighted sum of AADriskMulti's
+    risks on the same paths (to the rounding of the sum), and agrees with the generic kernel's aggregated adjoint
     (CF_FAST32=0) within 0.1 Monte Carlo standard error of each risk."""
     n = 1 << 16
     rs = np.random.RandomState(5)
@@ -44,6 +44,9 @@ def test_aggregate_fp32_through_the_portfolio_kernels(eng, portfolio, monkeypatc
     assert rel_to_max(a["risks"], m["risks"] @ w) < 1e-12
     assert rel_to_max(np.array([a["riskPayoffValue"]]), np.array([m["values"] @ w])) < 1e-12
     assert rel_to_max(a["payoffValues"], m["values"]) == 0.0
+    k = 37
+    one = eng.AADriskOne("c4dup", "c4port", num(sob, n, "fp32"), eng.payoffLabels("c4port")[k])
+    assert rel_to_max(one["risks"], m["risks"][:, k]) < 1e-12
     monkeypatch.setenv("CF_FAST32", "0")
     g = eng.AADriskAggregate("c4dup", "c4port", w, num(sob, n, "fp32"))
     monkeypatch.delenv("CF_FAST32")

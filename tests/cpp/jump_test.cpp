@@ -61,6 +61,22 @@ static void by_powers(const u64 g[9], u64 m, u64 v[3], u64 n)
     }
 }
 
+// The kernels' reduction (cf_device.cuh, mrg_matvec): each 32 x 32-bit product folded once with
+// 2^32 = C (mod m), the three of a row summed, two more folds and one conditional subtraction.
+template <u64 C, u64 M>
+static u64 folded_row(const u64 e[3], const u64 v[3])
+{
+    u64 s = 0;
+    for (int l = 0; l < 3; ++l)
+    {
+        const u64 q = e[l] * v[l];
+        s += (q >> 32) * C + (q & 0xffffffffULL);
+    }
+    s = (s >> 32) * C + (s & 0xffffffffULL);
+    s = (s >> 32) * C + (s & 0xffffffffULL);
+    return s >= M ? s - M : s;
+}
+
 static int failures = 0;
 static void check(bool c, const char* what, u64 n)
 {
@@ -106,6 +122,33 @@ int main()
         by_tables(B, M2, ty, n);
         check(tx[0] == x[0] && tx[1] == x[1] && tx[2] == x[2] && ty[0] == y[0] && ty[1] == y[1] && ty[2] == y[2],
               "tables_vs_powers", n);
+    }
+    // the folded reduction against exact arithmetic, at the extremes (entries and states up to m - 1)
+    // and on pseudo-random rows
+    {
+        bool ok = true;
+        u64 r = 88172645463325252ULL;
+        auto next = [&]() { r ^= r << 13; r ^= r >> 7; r ^= r << 17; return r; };
+        for (int it = 0; it < 200000 && ok; ++it)
+        {
+            u64 e1[3], v1[3], e2[3], v2[3];
+            for (int l = 0; l < 3; ++l)
+            {
+                const bool edge = it < 64;
+                e1[l] = edge ? M1 - 1 - (it >> l & 1) : next() % M1;
+                v1[l] = edge ? M1 - 1 - (it >> (l + 3) & 1) : next() % M1;
+                e2[l] = edge ? M2 - 1 - (it >> l & 1) : next() % M2;
+                v2[l] = edge ? M2 - 1 - (it >> (l + 3) & 1) : next() % M2;
+            }
+            unsigned __int128 x1 = 0, x2 = 0;
+            for (int l = 0; l < 3; ++l)
+            {
+                x1 += (unsigned __int128)e1[l] * v1[l];
+                x2 += (unsigned __int128)e2[l] * v2[l];
+            }
+            ok = folded_row<209, M1>(e1, v1) == u64(x1 % M1) && folded_row<22853, M2>(e2, v2) == u64(x2 % M2);
+        }
+        check(ok, "folded_reduction_exact", 200000);
     }
     return failures ? 1 : 0;
 }
